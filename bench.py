@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of the voxel SPH step on the 4M-particle box.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = hash, voxel sort, voxel table, density, forces, integrate and wall
+response for all 4,194,304 particles (128x256x128 dam break in a [0,2]^3 box,
+h = 0.0112, 5,735,339 voxels).  The state (~0.4 GB with both sort buffers) is
+larger than the 129 MB L2, so no flush is needed between steps.
+
+--impl gb300 (default): W untimed steps, then K steps timed with CUDA events
+(one CUDA-graph replay per step), barrier + synchronize on both sides, max over
+ranks.  Under torchrun each rank advances its own replica of the scene (the
+single scene does not shard; replicas only).  Also reported:
+  e2e      the same metric through the C ABI host-buffer entry point
+           (sphgb_compute_next_state_host): FP64 AoS state copied from pinned
+           host memory and the next state copied back, every step;
+  roofline the dominant kernel's algorithmic bytes / its mean CUDA-event time;
+  cpu_baseline  the oracle's C/OpenMP FP64 step on the host cores (rank 0).
+--impl reference: the reference's algorithm on the host cores (the oracle's
+C/OpenMP restatement; the reference itself is numba-CUDA Python and cannot run
+here), same metric; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "cuda-sph_gb300"), ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+# algorithmic bytes per particle of each stage (FP32 SoA, each array touched
+# once per pass): hash 16 + histogram 4; scan 8 per voxel (+4 clear);
+# scatter 8; rank-gather (reorder) 48; density 16; forces 40 + integrate/wall 60
+STAGE_BYTES_PER_PARTICLE = {"hash": 20, "scan": 0, "scatter": 8, "rank_gather": 48,
+                            "density": 16, "force_integrate": 100, "step_counter": 0}
+STAGE_BYTES_PER_VOXEL = {"hash": 4, "scan": 8}
+KERNELS_PER_STEP = 9   # hash, 3 scan, scatter, rank-gather, density, force+integrate, counter
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["config2", "config0"], default="config2")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-steps", type=int, default=2, help="oracle steps of the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name):
+    from sphgb import scenes
+    if name == "config2":
+        spec, st = scenes.config2()
+        desc = ("4M-particle dam-break box: 128x256x128 jittered lattice, spacing 0.005, "
+                "box [0,2]^3, h 0.0112, mass 1.25e-4, rho0 1000, K 3, visc 3.5, g -9.81, "
+                "restitution 0.5, dt 5e-4, 32-neighbour cap")
+    else:
+        spec, st = scenes.config0()
+        desc = "8k-particle dam-break box (16x32x16 lattice, h 0.045), 32-neighbour cap"
+    return spec, st, desc
+
+
+def dist_setup(args, backend):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def max_over_ranks(x, world, device=None):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms during a region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons, samples = [], [], set(), 0
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            samples += 1
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                pass
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": samples}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic(stage):
+    """DRAM bytes per launch of a stage's kernel from the committed ncu summary
+    (profiles/<kernel>_config2.txt, line 'traffic_bytes_per_launch: X')."""
+    names = {"force_integrate": "k_integrate", "density": "k_density",
+             "rank_gather": "k_rank_gather"}
+    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_config2.txt")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(spec, state, steps):
+    from oracle import ref
+    import numpy as np
+    sp = ref.params_from_spec(spec)
+    pos = np.ascontiguousarray(state.position, dtype=np.float64)
+    vel = np.ascontiguousarray(state.velocity, dtype=np.float64)
+    t0 = time.perf_counter()
+    for s in range(steps):
+        pos, vel, _ = ref.step(sp, pos, vel, step_index=s)
+    dt = time.perf_counter() - t0
+    return {"value": spec.n * steps / dt, "unit": "particle-steps/s", "cores": ref.num_threads(),
+            "kind": "port", "sample": f"{steps} full steps of the same {spec.n}-particle scene "
+                                     f"({dt:.1f} s wall, FP64 C/OpenMP restatement)"}
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_setup(args, "nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from sphgb.device import SceneBatch
+    spec, state, desc = workload(args.workload)
+    n = spec.n
+    batch = SceneBatch([spec], device=str(dev))
+    batch.load_states([state])
+    stream = torch.cuda.current_stream(dev)
+    # warm-up (also captures the one-step graph)
+    for _ in range(max(args.warmup, 0)):
+        batch.step(1, use_graph=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            batch.step(1, use_graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, world, dev)
+    value = n * args.steps * world / (ms / 1e3)
+    clocks = clk.summary()
+
+    # per-stage CUDA-event times (same kernels, no graph) -> dominant kernel roofline
+    stages = batch.step_profiled(min(args.steps, 10))
+    dom = max(("density", "force_integrate", "rank_gather", "hash", "scatter"),
+              key=lambda k: stages[k])
+    peak, peak_kind = measured_peak_hbm()
+    b_alg = STAGE_BYTES_PER_PARTICLE[dom] * n + STAGE_BYTES_PER_VOXEL.get(dom, 0) * batch.n_voxels
+    achieved = b_alg / (stages[dom] / 1e3) / 1e9
+    step_bytes = (192 * n + 12 * batch.n_voxels)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": committed_traffic(dom), "algorithmic_bytes": b_alg,
+                "kernel_ms": round(stages[dom], 4)}
+    step_roofline = {"algorithmic_bytes_per_step": step_bytes,
+                     "achieved": round(step_bytes / (ms / args.steps / 1e3) / 1e9, 1),
+                     "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
+                     "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
+
+    # end to end through the C ABI host-buffer entry point, pinned host memory
+    k_e2e = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 10)
+    pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa
+    h_pos = [pin((n, 3)), pin((n, 3))]
+    h_vel = [pin((n, 3)), pin((n, 3))]
+    h_rho = pin((n,))
+    h_pos[0][:] = state.position
+    h_vel[0][:] = state.velocity
+    batch.compute_next_state_host(h_pos[0], h_vel[0], h_pos[1], h_vel[1], h_rho)   # warm-up
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(k_e2e):
+        a, b = i % 2, (i + 1) % 2
+        batch.compute_next_state_host(h_pos[a], h_vel[a], h_pos[b], h_vel[b], h_rho)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, world, dev)
+    e2e = {"value": n * k_e2e * world / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 56 * n, "steps": k_e2e,
+           "api": "sphgb_compute_next_state_host"}
+    assert np.isfinite(h_pos[k_e2e % 2]).all()
+
+    out = {"metric": "particle-steps/s (4M box, 1 GB300)" if args.workload == "config2"
+           else "particle-steps/s (8k box)",
+           "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": desc, "particles": n, "voxels": batch.n_voxels,
+                      "l2": "inputs larger than L2 (state + sort buffers ~0.4 GB > 129 MB)",
+                      "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step"},
+           "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
+           "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(spec, state, args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    batch.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import ref
+    spec, state, desc = workload(args.workload)
+    sp = ref.params_from_spec(spec)
+    pos = np.ascontiguousarray(state.position, dtype=np.float64)
+    vel = np.ascontiguousarray(state.velocity, dtype=np.float64)
+    for s in range(min(args.warmup, 1)):
+        pos, vel, _ = ref.step(sp, pos, vel, step_index=s)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        pos, vel, _ = ref.step(sp, pos, vel, step_index=s)
+    dt = time.perf_counter() - t0
+    value = spec.n * args.steps / dt
+    cores = ref.num_threads()
+    out = {"impl": "reference",
+           "metric": "particle-steps/s (4M box, 1 GB300)" if args.workload == "config2"
+           else "particle-steps/s (8k box)",
+           "value": value, "unit": "particle-steps/s", "n_gpus": int(os.environ.get("WORLD_SIZE", 1)),
+           "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic",
+           "config": {"workload": desc, "particles": spec.n, "parallelism": "host cores"},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores,
+                            "kind": "port",
+                            "sample": f"{args.steps} full steps of the {spec.n}-particle scene"},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,916 @@
+// capi.cu -- the extern "C" boundary of libsphgb.so (declared in include/sphgb.h).
+//
+// A context (SphgbCtx) holds the scene descriptors, the pipe table and every
+// scratch buffer of the step; the caller owns the particle state and binds it.
+// The step enqueues, per time step:
+//   memset(voxel_count) -> hash+histogram -> scan -> scatter -> rank-gather
+//   -> density -> force+integrate+wall -> step counter
+// which is VoxelSPHStrategy.compute_next_state (sim/src/sph/strategies/
+// abstract_sph_strategy.py:31-46, voxel_sph_strategy.py:20-116) without any
+// host round trip.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sphgb_internal.cuh"
+
+#include "../../include/sphgb.h"
+
+using namespace sphgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(SPHGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SPHGB_CUDA(call)                                    \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+constexpr int kConsChunk = 1024;
+constexpr int kConsThreads = 256;
+constexpr int kConsFields = 8;
+
+struct ConsChunk {
+    int32_t scene, begin, end, pad;
+};
+
+}  // namespace
+
+struct SphgbCtx {
+    int device = 0;
+    int n_scenes = 0;
+    int n = 0;
+    int v_total = 0;
+    int n_tiles = 0;
+    bool any_pipe = false;
+    std::vector<SceneDev> h_scenes;
+    std::vector<int32_t> h_pbegin;
+    SceneDev* d_scenes = nullptr;
+    int32_t* d_pbegin = nullptr;
+    double* d_pipe = nullptr;
+    int n_pipe_rows = 0;
+    // scratch
+    int32_t* cell = nullptr;
+    int32_t* slot = nullptr;
+    int32_t* tmp_pid = nullptr;
+    int32_t* vstart = nullptr;
+    int32_t* vcount = nullptr;
+    int32_t* tile_sums = nullptr;
+    float4* posB = nullptr;
+    float4* velB = nullptr;
+    int32_t* pidB = nullptr;
+    double* pos64B = nullptr;
+    float2* aux = nullptr;
+    // bound (caller-owned) state
+    float4* posA = nullptr;
+    float4* velA = nullptr;
+    float* rho = nullptr;
+    int32_t* pidA = nullptr;
+    double* pos64A = nullptr;
+    int32_t* scene_step = nullptr;
+    bool bound = false;
+    // state owned by the context for the host-buffer entry point when nothing is bound
+    void* owned = nullptr;
+    // staging for the host-buffer entry point
+    double* stage = nullptr;
+    // conservation
+    int n_chunks = 0;
+    ConsChunk* d_chunks = nullptr;
+    double* d_partials = nullptr;
+    // streams and graphs
+    cudaStream_t cap_stream = nullptr;
+    cudaStream_t host_stream = nullptr;
+    std::map<int, cudaGraphExec_t> graphs;
+
+    Launch launch(cudaStream_t st) const {
+        Launch L;
+        L.scenes = d_scenes;
+        L.pbegin = d_pbegin;
+        L.n_scenes = n_scenes;
+        L.n = n;
+        L.v_total = v_total;
+        L.pipe = d_pipe;
+        L.stream = st;
+        return L;
+    }
+};
+
+namespace {
+
+template <class T>
+int dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(SPHGB_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return SPHGB_OK;
+}
+
+void free_ctx(SphgbCtx* c) {
+    if (!c) return;
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
+                    c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
+                    c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->host_stream) cudaStreamDestroy(c->host_stream);
+    delete c;
+}
+
+float round_down_f(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+
+float round_up_f(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
+int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d) {
+    std::memset(&d, 0, sizeof(d));
+    if (p.particle_count < 0) return fail(SPHGB_ERR_INVALID, "particle_count < 0");
+    if (!(p.inf_r > 0.0) || !std::isfinite(p.inf_r)) return fail(SPHGB_ERR_INVALID, "inf_r must be > 0");
+    if (!(p.dt > 0.0)) return fail(SPHGB_ERR_INVALID, "dt must be > 0");
+    if (p.mode != SPHGB_MODE_BOX && p.mode != SPHGB_MODE_PIPE)
+        return fail(SPHGB_ERR_INVALID, "mode must be SPHGB_MODE_BOX or SPHGB_MODE_PIPE");
+    if (p.walk_dims != SPHGB_WALK_CEIL && p.walk_dims != SPHGB_WALK_TRUNCATED)
+        return fail(SPHGB_ERR_INVALID, "walk_dims must be SPHGB_WALK_CEIL or SPHGB_WALK_TRUNCATED");
+    int64_t nv = 1;
+    for (int a = 0; a < 3; ++a) {
+        const double vs = (double)(float)p.voxel_size[a];
+        const double sp = (double)(float)p.space_size[a];
+        if (!(vs > 0.0) || !(sp > 0.0) || !std::isfinite(vs) || !std::isfinite(sp))
+            return fail(SPHGB_ERR_INVALID, "space_size and voxel_size must be finite and > 0");
+        const double q = sp / vs;
+        if (q > 1.0e7) return fail(SPHGB_ERR_RANGE, "space_size / voxel_size too large");
+        d.dims[a] = (int)std::ceil(q);                         // voxel_sph_strategy.py:70-73
+        if (d.dims[a] < 1) d.dims[a] = 1;
+        d.wdims[a] = p.walk_dims == SPHGB_WALK_TRUNCATED ? (int)q : d.dims[a];  // :110-116
+        d.vs[a] = (float)p.voxel_size[a];
+        d.space[a] = (float)p.space_size[a];
+        d.ext[a] = (float)p.external_force[a];
+        d.wall_hi[a] = (float)(p.space_size[a] - 1e-3);
+        nv *= d.dims[a];
+        if (nv > (int64_t)0x7fffffff) return fail(SPHGB_ERR_RANGE, "voxel table over 2^31 entries");
+    }
+    d.v_count = (int32_t)nv;
+    d.walk_trunc = (d.wdims[0] != d.dims[0] || d.wdims[1] != d.dims[1] || d.wdims[2] != d.dims[2]);
+    const float h = (float)p.inf_r;
+    const double hd = (double)h;
+    d.h = h;
+    d.h_d = hd;
+    const double h2 = hd * hd;  // exact
+    d.h2 = (float)h2;
+    d.h2_lo = round_down_f(h2 * (1.0 - std::ldexp(1.0, -18)));
+    d.h2_hi = round_up_f(h2 * (1.0 + std::ldexp(1.0, -18)));
+    d.cull2 = round_up_f((double)d.h2_hi * (1.0 + std::ldexp(1.0, -8)));
+    const double pi = 3.141592653589793;
+    // normalised kernel constants (config.py:27-29 times the power of h the
+    // kernels factor out): W_CONST h^6, GRAD_W_CONST h^2, LAP_W_CONST h
+    d.w_const = (float)(315.0 / (64.0 * pi * hd * hd * hd));
+    d.grad_w_const = (float)(-45.0 / (pi * hd * hd * hd * hd));
+    d.lap_w_const = (float)(45.0 / (pi * hd * hd * hd * hd * hd));
+    d.mass = (float)p.mass;
+    d.rho0 = (float)p.rho_0;
+    d.k = (float)p.k;
+    d.visc = (float)p.visc;
+    d.damp = (float)p.damp;
+    d.dt = (float)p.dt;
+    d.dt_d = p.dt;
+    d.wall_lo = (float)1e-3;
+    d.cap = p.max_neighbours > 0 ? p.max_neighbours : 0x7fffffff;
+    d.mode = p.mode;
+    d.seed = p.seed;
+    if (p.mode == SPHGB_MODE_PIPE) {
+        if (p.pipe_rows < 2) return fail(SPHGB_ERR_INVALID, "pipe mode needs >= 2 pipe rows");
+        if (p.pipe_row_offset < 0 || p.pipe_row_offset + p.pipe_rows > n_pipe_rows_total)
+            return fail(SPHGB_ERR_INVALID, "pipe rows outside the pipe table");
+        d.pipe_off = (int32_t)p.pipe_row_offset;
+        d.pipe_rows = p.pipe_rows;
+    }
+    return SPHGB_OK;
+}
+
+__global__ void k_load_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+                           int n_scenes, int n, const double* __restrict__ pos,
+                           const double* __restrict__ vel, float4* __restrict__ pos_out,
+                           float4* __restrict__ vel_out, int32_t* __restrict__ pid_out,
+                           double* __restrict__ pos64_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int si = scene_of(i, pbegin, n_scenes);
+    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    pos_out[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
+    vel_out[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
+    pid_out[i] = i - __ldg(pbegin + si);
+    if (pos64_out) {
+        // the accumulator starts from the FP32 state, as the device state does
+        pos64_out[3 * i] = (double)(float)x;
+        pos64_out[3 * i + 1] = (double)(float)y;
+        pos64_out[3 * i + 2] = (double)(float)z;
+    }
+    (void)scenes;
+}
+
+__global__ void k_store_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+                            int n_scenes, int n, const float4* __restrict__ pos,
+                            const float4* __restrict__ vel, const float* __restrict__ rho,
+                            const int32_t* __restrict__ pid, const double* __restrict__ pos64,
+                            double* __restrict__ pos_out, double* __restrict__ vel_out,
+                            double* __restrict__ rho_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int si = scene_of(s, pbegin, n_scenes);
+    const int i = __ldg(pbegin + si) + pid[s];
+    if (pos_out) {
+        if (pos64 && scenes[si].mode == 1) {
+            pos_out[3 * i] = pos64[3 * s];
+            pos_out[3 * i + 1] = pos64[3 * s + 1];
+            pos_out[3 * i + 2] = pos64[3 * s + 2];
+        } else {
+            const float4 p = pos[s];
+            pos_out[3 * i] = p.x;
+            pos_out[3 * i + 1] = p.y;
+            pos_out[3 * i + 2] = p.z;
+        }
+    }
+    if (vel_out) {
+        const float4 v = vel[s];
+        vel_out[3 * i] = v.x;
+        vel_out[3 * i + 1] = v.y;
+        vel_out[3 * i + 2] = v.z;
+    }
+    if (rho_out) rho_out[i] = rho ? (double)rho[s] : 0.0;
+}
+
+__global__ void k_step_counter(int32_t* scene_step, int n_scenes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_scenes) scene_step[i] += 1;
+}
+
+// values per sorted slot -> original particle order (scene offset + pid)
+__global__ void k_by_pid(const int32_t* __restrict__ pbegin, int n_scenes, int n,
+                         const int32_t* __restrict__ pid, const int32_t* __restrict__ a,
+                         const int32_t* __restrict__ b, int32_t* __restrict__ a_out,
+                         int32_t* __restrict__ b_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = __ldg(pbegin + scene_of(s, pbegin, n_scenes)) + pid[s];
+    if (a_out) a_out[i] = a[s];
+    if (b_out) b_out[i] = b[s];
+}
+
+// FP64 conservation sums, one block per chunk of one scene, fixed order.
+__global__ void __launch_bounds__(kConsThreads)
+k_cons_partial(const SceneDev* __restrict__ scenes, const ConsChunk* __restrict__ chunks,
+               const float4* __restrict__ pos, const float4* __restrict__ vel,
+               const double* __restrict__ pos64, double* __restrict__ partials) {
+    const ConsChunk ch = chunks[blockIdx.x];
+    const SceneDev& sc = scenes[ch.scene];
+    const double m = (double)sc.mass;
+    const double g0 = sc.ext[0], g1 = sc.ext[1], g2 = sc.ext[2];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int s = ch.begin + threadIdx.x; s < ch.end; s += kConsThreads) {
+        const float4 v = vel[s];
+        double x, y, z;
+        if (pos64 && sc.mode == 1) {
+            x = pos64[3 * s]; y = pos64[3 * s + 1]; z = pos64[3 * s + 2];
+        } else {
+            const float4 p = pos[s];
+            x = p.x; y = p.y; z = p.z;
+        }
+        const double vx = v.x, vy = v.y, vz = v.z;
+        acc[0] += m;
+        acc[1] += m * vx;
+        acc[2] += m * vy;
+        acc[3] += m * vz;
+        acc[4] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        acc[5] += -m * (g0 * x + g1 * y + g2 * z);
+    }
+    __shared__ double red[kConsThreads / 32][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        double v = acc[f];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[wid][f] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double v = 0.0;
+        for (int w = 0; w < kConsThreads / 32; ++w) v += red[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_cons_final(const ConsChunk* __restrict__ chunks, int n_chunks,
+                             const double* __restrict__ partials, const SceneDev* __restrict__ scenes,
+                             int n_scenes, double* __restrict__ out) {
+    const int si = blockIdx.x * blockDim.x + threadIdx.x;
+    if (si >= n_scenes) return;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < n_chunks; ++c) {
+        if (chunks[c].scene != si) continue;
+        for (int f = 0; f < 6; ++f) acc[f] += partials[(size_t)c * 6 + f];
+    }
+    double* o = out + (size_t)si * kConsFields;
+    o[0] = acc[0];
+    o[1] = acc[1];
+    o[2] = acc[2];
+    o[3] = acc[3];
+    o[4] = acc[4];
+    o[5] = acc[5];
+    o[6] = acc[4] + acc[5];
+    o[7] = (double)scenes[si].p_count;
+}
+
+// ---- pipe geometry wrappers (known-answer tests) ---------------------------
+__global__ void k_pipe_find(const double* pos, int n, const double* pipe, int rows, int32_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PipeView P{pipe, rows};
+    out[i] = pipe_find_segment(pos + 3 * i, P);
+}
+
+__global__ void k_pipe_is_out(const double* pos, const int32_t* seg, int n, const double* pipe,
+                              int rows, int32_t* out, double* radius) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PipeView P{pipe, rows};
+    double r = 0.0;
+    out[i] = pipe_is_out(pos + 3 * i, P, seg[i], &r) ? 1 : 0;
+    if (radius) radius[i] = r;
+}
+
+__global__ void k_pipe_xbegin(const int32_t* seg, int n, const double* pipe, int rows, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PipeView P{pipe, rows};
+    out[i] = pipe_x_begin(P, seg[i]);
+}
+
+__global__ void k_pipe_solve(double* pos, double* vel, int n, const double* pipe, int rows,
+                             int32_t* seg_out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PipeView P{pipe, rows};
+    double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    double v[3] = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+    const int s = pipe_find_segment(p, P);
+    if (seg_out) seg_out[i] = s;
+    if (s >= 0 && pipe_is_out(p, P, s, nullptr)) pipe_solve_collision(p, v, P, s);
+    for (int a = 0; a < 3; ++a) { pos[3 * i + a] = p[a]; vel[3 * i + a] = v[a]; }
+}
+
+__global__ void k_philox(uint64_t seed, const int32_t* pid, int n, int step, int draw, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = philox_uniform(seed, (uint32_t)pid[i], (uint32_t)step, (uint32_t)draw);
+}
+
+inline int blocks(int n, int b = kBlock) { return (n + b - 1) / b; }
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// enqueue one full step on stream st
+int enqueue_step(SphgbCtx* c, cudaStream_t st) {
+    const Launch L = c->launch(st);
+    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(c->vcount, 0, sizeof(int32_t) * c->v_total, st));
+    SPHGB_CUDA(launch_hash_count(L, c->posA, c->cell, c->slot, c->vcount));
+    SPHGB_CUDA(launch_scan(L, c->vcount, c->vstart, c->tile_sums, c->n_tiles));
+    SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, c->pidA, c->vstart, c->tmp_pid));
+    SPHGB_CUDA(launch_rank_gather(L, c->cell, c->pidA, c->tmp_pid, c->vstart, c->vcount, c->posA,
+                                  c->velA, c->any_pipe ? c->pos64A : nullptr, c->posB, c->velB,
+                                  c->pidB, c->any_pipe ? c->pos64B : nullptr));
+    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux));
+    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB,
+                                c->any_pipe ? c->pos64B : nullptr, c->vstart, c->vcount,
+                                c->scene_step, c->posA, c->velA, c->pidA,
+                                c->any_pipe ? c->pos64A : nullptr, nullptr));
+    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+// one step with an event after every stage: ev[0] before, ev[i+1] after stage i
+int enqueue_step_profiled(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev) {
+    const Launch L = c->launch(st);
+    SPHGB_CUDA(cudaEventRecord(ev[0], st));
+    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(c->vcount, 0, sizeof(int32_t) * c->v_total, st));
+    SPHGB_CUDA(launch_hash_count(L, c->posA, c->cell, c->slot, c->vcount));
+    SPHGB_CUDA(cudaEventRecord(ev[1], st));
+    SPHGB_CUDA(launch_scan(L, c->vcount, c->vstart, c->tile_sums, c->n_tiles));
+    SPHGB_CUDA(cudaEventRecord(ev[2], st));
+    SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, c->pidA, c->vstart, c->tmp_pid));
+    SPHGB_CUDA(cudaEventRecord(ev[3], st));
+    SPHGB_CUDA(launch_rank_gather(L, c->cell, c->pidA, c->tmp_pid, c->vstart, c->vcount, c->posA,
+                                  c->velA, c->any_pipe ? c->pos64A : nullptr, c->posB, c->velB,
+                                  c->pidB, c->any_pipe ? c->pos64B : nullptr));
+    SPHGB_CUDA(cudaEventRecord(ev[4], st));
+    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux));
+    SPHGB_CUDA(cudaEventRecord(ev[5], st));
+    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB,
+                                c->any_pipe ? c->pos64B : nullptr, c->vstart, c->vcount,
+                                c->scene_step, c->posA, c->velA, c->pidA,
+                                c->any_pipe ? c->pos64A : nullptr, nullptr));
+    SPHGB_CUDA(cudaEventRecord(ev[6], st));
+    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaEventRecord(ev[7], st));
+    return SPHGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphgb_abi_version(void) { return SPHGB_ABI_VERSION; }
+
+int sphgb_scene_params_size(void) { return (int)sizeof(SphgbSceneParams); }
+
+const char* sphgb_last_error(void) { return g_last_error.c_str(); }
+
+int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double* pipe_rows_table,
+                     int n_pipe_rows_total, SphgbCtx** out_ctx) {
+    if (!out_ctx) return fail(SPHGB_ERR_INVALID, "out_ctx is null");
+    *out_ctx = nullptr;
+    if (!scenes || n_scenes <= 0) return fail(SPHGB_ERR_INVALID, "need at least one scene");
+    if (n_pipe_rows_total < 0 || (n_pipe_rows_total > 0 && !pipe_rows_table))
+        return fail(SPHGB_ERR_INVALID, "bad pipe table");
+    SphgbCtx* c = new (std::nothrow) SphgbCtx();
+    if (!c) return fail(SPHGB_ERR_NOMEM, "host allocation failed");
+    cudaGetDevice(&c->device);
+    c->n_scenes = n_scenes;
+    c->h_scenes.resize(n_scenes);
+    c->h_pbegin.resize(n_scenes + 1);
+    int64_t n_tot = 0, v_tot = 0;
+    for (int i = 0; i < n_scenes; ++i) {
+        int rc = build_scene(scenes[i], n_pipe_rows_total, c->h_scenes[i]);
+        if (rc) {
+            free_ctx(c);
+            return fail(rc, "scene " + std::to_string(i) + ": " + g_last_error);
+        }
+        SceneDev& d = c->h_scenes[i];
+        d.p_begin = (int32_t)n_tot;
+        d.p_count = (int32_t)scenes[i].particle_count;
+        d.v_begin = (int32_t)v_tot;
+        c->h_pbegin[i] = (int32_t)n_tot;
+        n_tot += scenes[i].particle_count;
+        v_tot += d.v_count;
+        if (n_tot > (int64_t)0x7fffffff - 1 || v_tot > (int64_t)0x7fffffff - 1) {
+            free_ctx(c);
+            return fail(SPHGB_ERR_RANGE, "particles or voxels over 2^31 in one context");
+        }
+        if (d.mode == SPHGB_MODE_PIPE) c->any_pipe = true;
+    }
+    c->h_pbegin[n_scenes] = (int32_t)n_tot;
+    c->n = (int)n_tot;
+    c->v_total = (int)v_tot;
+    c->n_tiles = scan_tiles(c->v_total);
+    c->n_pipe_rows = n_pipe_rows_total;
+    // conservation chunks
+    std::vector<ConsChunk> chunks;
+    for (int i = 0; i < n_scenes; ++i) {
+        const SceneDev& d = c->h_scenes[i];
+        for (int b = 0; b < d.p_count; b += kConsChunk)
+            chunks.push_back({i, d.p_begin + b, d.p_begin + std::min(d.p_count, b + kConsChunk), 0});
+    }
+    c->n_chunks = (int)chunks.size();
+    const size_t N = (size_t)c->n, V = (size_t)c->v_total;
+    int rc = SPHGB_OK;
+    rc = rc ? rc : dalloc(&c->d_scenes, (size_t)n_scenes);
+    rc = rc ? rc : dalloc(&c->d_pbegin, (size_t)n_scenes + 1);
+    rc = rc ? rc : dalloc(&c->d_pipe, (size_t)n_pipe_rows_total * 5);
+    rc = rc ? rc : dalloc(&c->cell, N);
+    rc = rc ? rc : dalloc(&c->slot, N);
+    rc = rc ? rc : dalloc(&c->tmp_pid, N);
+    rc = rc ? rc : dalloc(&c->vstart, V);
+    rc = rc ? rc : dalloc(&c->vcount, V);
+    rc = rc ? rc : dalloc(&c->tile_sums, (size_t)c->n_tiles);
+    rc = rc ? rc : dalloc(&c->posB, N);
+    rc = rc ? rc : dalloc(&c->velB, N);
+    rc = rc ? rc : dalloc(&c->pidB, N);
+    rc = rc ? rc : dalloc(&c->aux, N);
+    if (c->any_pipe) rc = rc ? rc : dalloc(&c->pos64B, 3 * N);
+    rc = rc ? rc : dalloc(&c->d_chunks, chunks.size());
+    rc = rc ? rc : dalloc(&c->d_partials, chunks.size() * 6);
+    if (rc) {
+        std::string m = g_last_error;
+        free_ctx(c);
+        return fail(rc, m);
+    }
+    cudaError_t e = cudaMemcpy(c->d_scenes, c->h_scenes.data(), sizeof(SceneDev) * n_scenes,
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c->d_pbegin, c->h_pbegin.data(), sizeof(int32_t) * (n_scenes + 1),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_pipe_rows_total > 0)
+        e = cudaMemcpy(c->d_pipe, pipe_rows_table, sizeof(double) * 5 * n_pipe_rows_total,
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !chunks.empty())
+        e = cudaMemcpy(c->d_chunks, chunks.data(), sizeof(ConsChunk) * chunks.size(),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_ctx(c);
+        return cuda_fail(e, "sphgb_ctx_create");
+    }
+    *out_ctx = c;
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_destroy(SphgbCtx* ctx) {
+    if (!ctx) return SPHGB_OK;
+    cudaDeviceSynchronize();
+    free_ctx(ctx);
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_sizes(const SphgbCtx* ctx, int64_t* n_particles, int64_t* n_voxels) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (n_particles) *n_particles = ctx->n;
+    if (n_voxels) *n_voxels = ctx->v_total;
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_bind_state(SphgbCtx* ctx, float* d_pos, float* d_vel, float* d_rho, int32_t* d_pid,
+                         double* d_pos64, int32_t* d_scene_step) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos || !d_vel || !d_rho || !d_pid))
+        return fail(SPHGB_ERR_INVALID, "state pointers must not be null");
+    if (!d_scene_step) return fail(SPHGB_ERR_INVALID, "scene_step must not be null");
+    if (ctx->any_pipe && ctx->n > 0 && !d_pos64)
+        return fail(SPHGB_ERR_INVALID, "pipe scenes need the FP64 position buffer");
+    if (((uintptr_t)d_pos | (uintptr_t)d_vel) & 15u)
+        return fail(SPHGB_ERR_INVALID, "position/velocity buffers must be 16-byte aligned");
+    ctx->posA = reinterpret_cast<float4*>(d_pos);
+    ctx->velA = reinterpret_cast<float4*>(d_vel);
+    ctx->rho = d_rho;
+    ctx->pidA = d_pid;
+    ctx->pos64A = ctx->any_pipe ? d_pos64 : nullptr;
+    ctx->scene_step = d_scene_step;
+    ctx->bound = true;
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double* d_vel_aos,
+                           void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    if (ctx->n == 0) return SPHGB_OK;
+    if (!d_pos_aos || !d_vel_aos) return fail(SPHGB_ERR_INVALID, "null input");
+    cudaStream_t st = as_stream(stream);
+    k_load_aos<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes,
+                                                 ctx->n, d_pos_aos, d_vel_aos, ctx->posA,
+                                                 ctx->velA, ctx->pidA, ctx->pos64A);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos, double* d_rho,
+                            void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    if (ctx->n == 0) return SPHGB_OK;
+    cudaStream_t st = as_stream(stream);
+    k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes,
+                                                  ctx->n, ctx->posA, ctx->velA, ctx->rho,
+                                                  ctx->pidA, ctx->pos64A, d_pos_aos, d_vel_aos,
+                                                  d_rho);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_step(SphgbCtx* ctx, int n_steps, int use_graph, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    if (n_steps < 0) return fail(SPHGB_ERR_INVALID, "n_steps < 0");
+    if (n_steps == 0 || ctx->n == 0) return SPHGB_OK;
+    cudaStream_t st = as_stream(stream);
+    if (!use_graph) {
+        for (int i = 0; i < n_steps; ++i) {
+            int rc = enqueue_step(ctx, st);
+            if (rc) return rc;
+        }
+        return SPHGB_OK;
+    }
+    auto it = ctx->graphs.find(n_steps);
+    if (it == ctx->graphs.end()) {
+        SPHGB_CUDA(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeThreadLocal));
+        int rc = SPHGB_OK;
+        for (int i = 0; i < n_steps && rc == SPHGB_OK; ++i) rc = enqueue_step(ctx, ctx->cap_stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        cudaGraphExec_t ex = nullptr;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        it = ctx->graphs.emplace(n_steps, ex).first;
+    }
+    SPHGB_CUDA(cudaGraphLaunch(it->second, st));
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_stage_ms) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    if (n_steps < 0 || !h_stage_ms) return fail(SPHGB_ERR_INVALID, "bad arguments");
+    for (int i = 0; i < SPHGB_PROFILE_STAGES; ++i) h_stage_ms[i] = 0.0f;
+    if (n_steps == 0 || ctx->n == 0) return SPHGB_OK;
+    cudaStream_t st = as_stream(stream);
+    std::vector<cudaEvent_t> ev((size_t)n_steps * 8, nullptr);
+    int rc = SPHGB_OK;
+    for (auto& e : ev) {
+        cudaError_t err = cudaEventCreate(&e);
+        if (err != cudaSuccess) { rc = cuda_fail(err, "cudaEventCreate"); break; }
+    }
+    for (int i = 0; i < n_steps && rc == SPHGB_OK; ++i) rc = enqueue_step_profiled(ctx, st, &ev[(size_t)i * 8]);
+    if (rc == SPHGB_OK) {
+        cudaError_t err = cudaStreamSynchronize(st);
+        if (err != cudaSuccess) rc = cuda_fail(err, "cudaStreamSynchronize");
+    }
+    for (int i = 0; i < n_steps && rc == SPHGB_OK; ++i)
+        for (int k = 0; k < SPHGB_PROFILE_STAGES; ++k) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[(size_t)i * 8 + k], ev[(size_t)i * 8 + k + 1]);
+            h_stage_ms[k] += ms / (float)n_steps;
+        }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return rc;
+}
+
+int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
+                                  double* h_pos_out, double* h_vel_out, double* h_rho_out) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n_scenes != 1) return fail(SPHGB_ERR_INVALID, "host entry needs a one-scene context");
+    const size_t N = (size_t)ctx->n;
+    if (N > 0 && (!h_pos || !h_vel || !h_pos_out || !h_vel_out || !h_rho_out))
+        return fail(SPHGB_ERR_INVALID, "null host buffer");
+    if (!ctx->bound) {
+        // own state: pos, vel (float4), rho, pid, pos64, scene_step
+        const size_t bytes = N * 16 * 2 + N * 4 * 2 + (ctx->any_pipe ? N * 24 : 0) + 16;
+        if (!ctx->owned) {
+            cudaError_t e = cudaMalloc(&ctx->owned, bytes);
+            if (e != cudaSuccess) {
+                ctx->owned = nullptr;
+                return fail(SPHGB_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+            }
+            SPHGB_CUDA(cudaMemset(ctx->owned, 0, bytes));
+        }
+        char* b = static_cast<char*>(ctx->owned);
+        float* pos = reinterpret_cast<float*>(b);
+        float* vel = reinterpret_cast<float*>(b + N * 16);
+        float* rho = reinterpret_cast<float*>(b + N * 32);
+        int32_t* pid = reinterpret_cast<int32_t*>(b + N * 36);
+        double* pos64 = ctx->any_pipe ? reinterpret_cast<double*>(b + N * 40) : nullptr;
+        int32_t* step = reinterpret_cast<int32_t*>(b + N * 40 + (ctx->any_pipe ? N * 24 : 0));
+        int rc = sphgb_ctx_bind_state(ctx, pos, vel, rho, pid, pos64, step);
+        if (rc) return rc;
+    }
+    if (N == 0) return SPHGB_OK;
+    if (!ctx->stage) {
+        cudaError_t e = cudaMalloc(&ctx->stage, sizeof(double) * N * 7);
+        if (e != cudaSuccess) {
+            ctx->stage = nullptr;
+            return fail(SPHGB_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaStream_t st = ctx->host_stream;
+    double* sp = ctx->stage;
+    double* sv = ctx->stage + 3 * N;
+    double* sr = ctx->stage + 6 * N;
+    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    int rc = sphgb_ctx_load_aos_f64(ctx, sp, sv, st);
+    if (rc) return rc;
+    rc = enqueue_step(ctx, st);
+    if (rc) return rc;
+    rc = sphgb_ctx_store_aos_f64(ctx, sp, sv, sr, st);
+    if (rc) return rc;
+    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaStreamSynchronize(st));
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_conservation(SphgbCtx* ctx, double* d_out, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    if (!d_out) return fail(SPHGB_ERR_INVALID, "d_out is null");
+    cudaStream_t st = as_stream(stream);
+    if (ctx->n_chunks > 0)
+        k_cons_partial<<<ctx->n_chunks, kConsThreads, 0, st>>>(ctx->d_scenes, ctx->d_chunks,
+                                                               ctx->posA, ctx->velA, ctx->pos64A,
+                                                               ctx->d_partials);
+    k_cons_final<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->d_chunks, ctx->n_chunks,
+                                                            ctx->d_partials, ctx->d_scenes,
+                                                            ctx->n_scenes, d_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_uncapped, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
+    cudaStream_t st = as_stream(stream);
+    const Launch L = ctx->launch(st);
+    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * ctx->v_total, st));
+    SPHGB_CUDA(launch_hash_count(L, ctx->posA, ctx->cell, ctx->slot, ctx->vcount));
+    SPHGB_CUDA(launch_scan(L, ctx->vcount, ctx->vstart, ctx->tile_sums, ctx->n_tiles));
+    SPHGB_CUDA(launch_scatter(L, ctx->cell, ctx->slot, ctx->pidA, ctx->vstart, ctx->tmp_pid));
+    SPHGB_CUDA(launch_rank_gather(L, ctx->cell, ctx->pidA, ctx->tmp_pid, ctx->vstart, ctx->vcount,
+                                  ctx->posA, ctx->velA, ctx->any_pipe ? ctx->pos64A : nullptr,
+                                  ctx->posB, ctx->velB, ctx->pidB,
+                                  ctx->any_pipe ? ctx->pos64B : nullptr));
+    // per sorted slot into the scratch id buffers, then to original order
+    SPHGB_CUDA(launch_neighbours(L, ctx->posB, ctx->vstart, ctx->vcount, nullptr, 0, ctx->cell,
+                                 ctx->slot));
+    k_by_pid<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n, ctx->pidB,
+                                                ctx->cell, ctx->slot, d_capped, d_uncapped);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_assign_voxels(SphgbCtx* ctx, const float* d_pos, int32_t* d_voxel_out, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos || !d_voxel_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
+    cudaStream_t st = as_stream(stream);
+    const Launch L = ctx->launch(st);
+    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * ctx->v_total, st));
+    SPHGB_CUDA(launch_hash_count(L, reinterpret_cast<const float4*>(d_pos), d_voxel_out, ctx->slot,
+                                 ctx->vcount));
+    return SPHGB_OK;
+}
+
+int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
+                          const int32_t* d_pid, const double* d_pos64, float* d_pos_out,
+                          float* d_vel_out, int32_t* d_pid_out, double* d_pos64_out,
+                          int32_t* d_voxel_start, int32_t* d_voxel_count, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos || !d_vel || !d_pid || !d_pos_out || !d_vel_out || !d_pid_out))
+        return fail(SPHGB_ERR_INVALID, "null buffer");
+    if (!d_voxel_start || !d_voxel_count) return fail(SPHGB_ERR_INVALID, "null voxel table");
+    if ((d_pos64 == nullptr) != (d_pos64_out == nullptr))
+        return fail(SPHGB_ERR_INVALID, "pass both FP64 position buffers or neither");
+    cudaStream_t st = as_stream(stream);
+    const Launch L = ctx->launch(st);
+    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(d_voxel_count, 0, sizeof(int32_t) * ctx->v_total, st));
+    SPHGB_CUDA(launch_hash_count(L, reinterpret_cast<const float4*>(d_pos), ctx->cell, ctx->slot,
+                                 d_voxel_count));
+    SPHGB_CUDA(launch_scan(L, d_voxel_count, d_voxel_start, ctx->tile_sums, ctx->n_tiles));
+    SPHGB_CUDA(launch_scatter(L, ctx->cell, ctx->slot, d_pid, d_voxel_start, ctx->tmp_pid));
+    SPHGB_CUDA(launch_rank_gather(L, ctx->cell, d_pid, ctx->tmp_pid, d_voxel_start, d_voxel_count,
+                                  reinterpret_cast<const float4*>(d_pos),
+                                  reinterpret_cast<const float4*>(d_vel), d_pos64,
+                                  reinterpret_cast<float4*>(d_pos_out),
+                                  reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out));
+    return SPHGB_OK;
+}
+
+int sphgb_neighbours(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_voxel_start,
+                     const int32_t* d_voxel_count, int32_t* d_list, int list_stride,
+                     int32_t* d_count_capped, int32_t* d_count_uncapped, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (d_list && list_stride <= 0) return fail(SPHGB_ERR_INVALID, "list_stride must be > 0");
+    cudaStream_t st = as_stream(stream);
+    SPHGB_CUDA(launch_neighbours(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
+                                 d_voxel_start, d_voxel_count, d_list, list_stride, d_count_capped,
+                                 d_count_uncapped));
+    return SPHGB_OK;
+}
+
+int sphgb_density(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_voxel_start,
+                  const int32_t* d_voxel_count, float* d_rho_out, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos_sorted || !d_rho_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
+    cudaStream_t st = as_stream(stream);
+    SPHGB_CUDA(launch_density(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
+                              d_voxel_start, d_voxel_count, d_rho_out, ctx->aux));
+    return SPHGB_OK;
+}
+
+int sphgb_forces(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_sorted,
+                 const float* d_rho_sorted, const int32_t* d_voxel_start,
+                 const int32_t* d_voxel_count, float* d_pressure_out, float* d_viscosity_out,
+                 void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos_sorted || !d_vel_sorted || !d_rho_sorted || !d_pressure_out ||
+                       !d_viscosity_out))
+        return fail(SPHGB_ERR_INVALID, "null buffer");
+    cudaStream_t st = as_stream(stream);
+    const Launch L = ctx->launch(st);
+    SPHGB_CUDA(launch_aux_from_rho(L, d_rho_sorted, ctx->aux));
+    SPHGB_CUDA(launch_forces(L, reinterpret_cast<const float4*>(d_pos_sorted),
+                             reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted, ctx->aux,
+                             d_voxel_start, d_voxel_count, reinterpret_cast<float4*>(d_pressure_out),
+                             reinterpret_cast<float4*>(d_viscosity_out)));
+    return SPHGB_OK;
+}
+
+int sphgb_integrate(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_sorted,
+                    const float* d_rho_sorted, const int32_t* d_pid_sorted,
+                    const double* d_pos64_sorted, const int32_t* d_voxel_start,
+                    const int32_t* d_voxel_count, const int32_t* d_scene_step, float* d_pos_out,
+                    float* d_vel_out, int32_t* d_pid_out, double* d_pos64_out, float* d_force_out,
+                    void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (ctx->n > 0 && (!d_pos_sorted || !d_vel_sorted || !d_rho_sorted || !d_pid_sorted ||
+                       !d_pos_out || !d_vel_out || !d_pid_out || !d_scene_step))
+        return fail(SPHGB_ERR_INVALID, "null buffer");
+    if (ctx->any_pipe && ctx->n > 0 && (!d_pos64_sorted || !d_pos64_out))
+        return fail(SPHGB_ERR_INVALID, "pipe scenes need the FP64 position buffers");
+    cudaStream_t st = as_stream(stream);
+    const Launch L = ctx->launch(st);
+    SPHGB_CUDA(launch_aux_from_rho(L, d_rho_sorted, ctx->aux));
+    SPHGB_CUDA(launch_integrate(L, reinterpret_cast<const float4*>(d_pos_sorted),
+                                reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
+                                ctx->aux, d_pid_sorted, d_pos64_sorted, d_voxel_start,
+                                d_voxel_count, d_scene_step, reinterpret_cast<float4*>(d_pos_out),
+                                reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out,
+                                reinterpret_cast<float4*>(d_force_out)));
+    return SPHGB_OK;
+}
+
+int sphgb_pipe_find_segment(const double* d_pos, int n, const double* d_pipe, int pipe_rows,
+                            int32_t* d_seg_out, void* stream) {
+    if (n < 0 || pipe_rows < 2) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (n == 0) return SPHGB_OK;
+    k_pipe_find<<<blocks(n), kBlock, 0, as_stream(stream)>>>(d_pos, n, d_pipe, pipe_rows, d_seg_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_pipe_is_out(const double* d_pos, const int32_t* d_seg, int n, const double* d_pipe,
+                      int pipe_rows, int32_t* d_out, double* d_radius_out, void* stream) {
+    if (n < 0 || pipe_rows < 2) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (n == 0) return SPHGB_OK;
+    k_pipe_is_out<<<blocks(n), kBlock, 0, as_stream(stream)>>>(d_pos, d_seg, n, d_pipe, pipe_rows,
+                                                               d_out, d_radius_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_pipe_x_at_segment_beginning(const int32_t* d_seg, int n, const double* d_pipe,
+                                      int pipe_rows, double* d_out, void* stream) {
+    if (n < 0 || pipe_rows < 1) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (n == 0) return SPHGB_OK;
+    k_pipe_xbegin<<<blocks(n), kBlock, 0, as_stream(stream)>>>(d_seg, n, d_pipe, pipe_rows, d_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_pipe_solve_collision(double* d_pos, double* d_vel, int n, const double* d_pipe,
+                               int pipe_rows, int32_t* d_seg_out, void* stream) {
+    if (n < 0 || pipe_rows < 2) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (n == 0) return SPHGB_OK;
+    k_pipe_solve<<<blocks(n), kBlock, 0, as_stream(stream)>>>(d_pos, d_vel, n, d_pipe, pipe_rows,
+                                                              d_seg_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_philox_uniform(uint64_t seed, const int32_t* d_pid, int n, int step, int draw,
+                         double* d_out, void* stream) {
+    if (n < 0) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (n == 0) return SPHGB_OK;
+    k_philox<<<blocks(n), kBlock, 0, as_stream(stream)>>>(seed, d_pid, n, step, draw, d_out);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,231 @@
+// sort.cu -- voxel hash, counting sort and voxel table.
+//
+// Replaces the host-side voxel organisation of the reference
+// (sim/src/sph/strategies/voxel_sph_strategy.py:65-107: GPU hash, copy to the
+// host, numpy structured sort by (voxel_id, particle_id), Python loop building
+// voxel_begin) with four device passes:
+//   1. hash: voxel id per particle + atomic histogram (slot = arrival rank);
+//   2. scan: exclusive prefix of the histogram = voxel_start (tile sums, one
+//      scan of the tile sums, tile-local warp-shuffle scans);
+//   3. scatter: particle id of each particle to voxel_start + slot;
+//   4. rank-gather: each particle's final slot = voxel_start + number of
+//      members of its voxel with a smaller particle id; the state is gathered
+//      into that slot.  The result is the reference's (voxel, particle id)
+//      order exactly, independent of atomic arrival order and of the input
+//      order of the state.
+#include "sphgb_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;  // 4096 voxels per tile
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// exclusive scan of one int per thread across the block; `total` receives the
+// block total.  Safe to call repeatedly if the caller synchronises between calls.
+__device__ __forceinline__ int block_excl_scan(int v, int& total) {
+    constexpr int kWarps = kScanThreads / 32;
+    __shared__ int warp_off[kWarps];
+    __shared__ int block_total;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int incl = warp_incl_scan(v);
+    if (lane == 31) warp_off[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int w = lane < kWarps ? warp_off[lane] : 0;
+        const int wi = warp_incl_scan(w);
+        if (lane < kWarps) warp_off[lane] = wi - w;
+        if (lane == kWarps - 1) block_total = wi;
+    }
+    __syncthreads();
+    total = block_total;
+    return incl - v + warp_off[wid];
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+             int n, const float4* __restrict__ pos, int32_t* __restrict__ cell,
+             int32_t* __restrict__ slot, int32_t* __restrict__ vcount) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const float4 p = __ldg(pos + s);
+    const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
+    const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
+    const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
+    const int vid = sc.v_begin + vx + vy * sc.dims[0] + vz * sc.dims[0] * sc.dims[1];
+    cell[s] = vid;
+    slot[s] = atomicAdd(vcount + vid, 1);
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_tile_reduce(const int32_t* __restrict__ vcount, int v_total, int32_t* __restrict__ tile_sums) {
+    const int base = blockIdx.x * kScanTile;
+    int sum = 0;
+    if (base + kScanTile <= v_total) {
+        const int4* v4 = reinterpret_cast<const int4*>(vcount + base);
+#pragma unroll
+        for (int i = 0; i < kScanItems / 4; ++i) {
+            int4 q = __ldg(v4 + threadIdx.x + i * kScanThreads);
+            sum += q.x + q.y + q.z + q.w;
+        }
+    } else {
+        for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+            int k = base + i;
+            if (k < v_total) sum += __ldg(vcount + k);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    __shared__ int ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int v = threadIdx.x < kScanThreads / 32 ? ws[threadIdx.x] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) tile_sums[blockIdx.x] = v;
+    }
+}
+
+// one block: exclusive scan of the tile sums in place
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_tile_sums(int32_t* __restrict__ tile_sums, int n_tiles) {
+    int carry = 0;
+    for (int base = 0; base < n_tiles; base += kScanThreads) {
+        const int i = base + threadIdx.x;
+        const int v = i < n_tiles ? tile_sums[i] : 0;
+        int total = 0;
+        const int ex = block_excl_scan(v, total);
+        if (i < n_tiles) tile_sums[i] = carry + ex;
+        carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_tile_scan(const int32_t* __restrict__ vcount, int v_total, const int32_t* __restrict__ tile_prefix,
+            int32_t* __restrict__ vstart) {
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    const bool full = (blockIdx.x + 1) * kScanTile <= v_total;
+    if (full) {
+        const int4* v4 = reinterpret_cast<const int4*>(vcount + base);
+#pragma unroll
+        for (int i = 0; i < kScanItems / 4; ++i) {
+            int4 q = __ldg(v4 + i);
+            v[4 * i] = q.x; v[4 * i + 1] = q.y; v[4 * i + 2] = q.z; v[4 * i + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) v[i] = base + i < v_total ? __ldg(vcount + base + i) : 0;
+    }
+    int tsum = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) tsum += v[i];
+    int total = 0;
+    int run = block_excl_scan(tsum, total) + __ldg(tile_prefix + blockIdx.x);
+    int out[kScanItems];
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) { out[i] = run; run += v[i]; }
+    if (full) {
+        int4* o4 = reinterpret_cast<int4*>(vstart + base);
+#pragma unroll
+        for (int i = 0; i < kScanItems / 4; ++i)
+            o4[i] = make_int4(out[4 * i], out[4 * i + 1], out[4 * i + 2], out[4 * i + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) if (base + i < v_total) vstart[base + i] = out[i];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_scatter(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ slot,
+          const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
+          int32_t* __restrict__ tmp_pid) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    tmp_pid[__ldg(vstart + cell[s]) + slot[s]] = pid[s];
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ pid,
+              const int32_t* __restrict__ tmp_pid, const int32_t* __restrict__ vstart,
+              const int32_t* __restrict__ vcount, const float4* __restrict__ pos,
+              const float4* __restrict__ vel, const double* __restrict__ pos64,
+              float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+              int32_t* __restrict__ pid_out, double* __restrict__ pos64_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int vid = cell[s];
+    const int p = pid[s];
+    const int st = __ldg(vstart + vid);
+    const int c = __ldg(vcount + vid);
+    int r = 0;
+    for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
+    const int d = st + r;
+    pid_out[d] = p;
+    pos_out[d] = __ldg(pos + s);
+    vel_out[d] = __ldg(vel + s);
+    if (pos64) {
+        pos64_out[3 * d + 0] = pos64[3 * s + 0];
+        pos64_out[3 * d + 1] = pos64[3 * s + 1];
+        pos64_out[3 * d + 2] = pos64[3 * s + 2];
+    }
+}
+
+inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+}  // namespace
+
+int scan_tiles(int v_total) { return (v_total + kScanTile - 1) / kScanTile; }
+
+cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
+                              int32_t* vcount) {
+    if (L.n == 0) return cudaSuccess;
+    k_hash_count<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n,
+                                                            pos, cell, slot, vcount);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
+                        int32_t* tile_sums, int n_tiles) {
+    if (L.v_total == 0) return cudaSuccess;
+    k_tile_reduce<<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums);
+    k_scan_tile_sums<<<1, kScanThreads, 0, L.stream>>>(tile_sums, n_tiles);
+    k_tile_scan<<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums, vstart);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* slot,
+                           const int32_t* pid, const int32_t* vstart, int32_t* tmp_pid) {
+    if (L.n == 0) return cudaSuccess;
+    k_scatter<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, slot, pid, vstart, tmp_pid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
+                               const int32_t* tmp_pid, const int32_t* vstart,
+                               const int32_t* vcount, const float4* pos, const float4* vel,
+                               const double* pos64, float4* pos_out, float4* vel_out,
+                               int32_t* pid_out, double* pos64_out) {
+    if (L.n == 0) return cudaSuccess;
+    k_rank_gather<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart,
+                                                             vcount, pos, vel, pos64, pos_out,
+                                                             vel_out, pid_out, pos64_out);
+    return cudaGetLastError();
+}
+
+}  // namespace sphgb

@@ -1,0 +1,360 @@
+// sphgb_internal.cuh -- device-side building blocks shared by the kernels.
+//
+// Numerical contract (matches an FP64 evaluation of the reference on FP32
+// inputs; reference = iwoplaza/cuda-sph, sim/src/sph/kernels/*.py):
+//  * voxel coordinate: floor(x / voxel) computed exactly for FP32 x, voxel
+//    (rounded quotient corrected by an exact fma residual).  For FP32 inputs
+//    this equals the reference's int32(x / voxel) in FP64
+//    (voxel_kernels.py:10-12) for 0 <= x; coordinates are clamped to the table.
+//  * neighbour test sqrt(dx^2 + dy^2 + dz^2) <= INF_R (voxel_kernels.py:20-26):
+//    evaluated in FP32 with a relative guard band of 2^-18 around h^2; inside
+//    the band it is re-evaluated in FP64 exactly as the reference writes it
+//    (no contraction, same operation order), so the decision is identical to
+//    the FP64 one.  The FP32 error of d^2 is below 2^-21 relative.
+//  * the physics sums (density, pressure, viscosity) are FP32 with Kahan
+//    compensation; FP64 is used only in the guard band, the pipe-flow position
+//    accumulator with its wall response, and the conservation reductions.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphgb {
+
+constexpr int kBlock = 256;
+
+// One scene as the kernels see it (built on the host from SphgbSceneParams).
+struct SceneDev {
+    int32_t p_begin, p_count;   // slots [p_begin, p_begin + p_count) in sorted state
+    int32_t v_begin, v_count;   // voxel table range
+    int32_t dims[3];            // table dims, ceil(space / voxel)
+    int32_t wdims[3];           // walk dims (== dims, or truncated)
+    float vs[3];                // voxel size
+    float h, h2, h2_lo, h2_hi;  // INF_R, INF_R^2 and the FP32 guard band
+    float cull2;                // squared distance beyond which a voxel is skipped
+    float w_const, grad_w_const, lap_w_const;
+    float mass, rho0, k, visc, damp, dt;
+    float ext[3];
+    float space[3];
+    float wall_lo, wall_hi[3];  // 1e-3 and space - 1e-3 (base_kernels.py:75-98)
+    double h_d;                 // (double)h for the guard-band path
+    double dt_d;
+    int32_t cap;                // MAX_NEIGHBOURS, or a huge value when uncapped
+    int32_t mode;               // 0 box, 1 pipe
+    int32_t walk_trunc;         // 1 when wdims != dims (no voxel culling then)
+    int32_t pipe_off, pipe_rows;
+    int32_t pad;
+    uint64_t seed;
+};
+
+// ---- scene lookup ---------------------------------------------------------
+// pbegin has n_scenes + 1 entries (prefix of particle counts).
+__device__ __forceinline__ int scene_of(int s, const int32_t* __restrict__ pbegin, int n_scenes) {
+    int lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (__ldg(pbegin + mid) <= s) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- exact voxel coordinate ----------------------------------------------
+__device__ __forceinline__ int voxel_coord(float x, float vs, int dim) {
+    if (!(x >= 0.0f)) return 0;                  // negative or NaN: first voxel
+    float q = floorf(__fdiv_rn(x, vs));
+    // the rounded quotient is floor(x/vs) or one more; the sign of the exact
+    // residual x - q*vs (one rounding, sign preserved) decides
+    if (__fmaf_rn(-q, vs, x) < 0.0f) q -= 1.0f;
+    if (q >= (float)dim) return dim - 1;
+    return (int)q;
+}
+
+// ---- neighbour predicate --------------------------------------------------
+static __device__ __noinline__ bool within_exact(float xi, float yi, float zi, float xj, float yj,
+                                          float zj, double h) {
+    double dx = __dsub_rn((double)xi, (double)xj);
+    double dy = __dsub_rn((double)yi, (double)yj);
+    double dz = __dsub_rn((double)zi, (double)zj);
+    double s = __dmul_rn(dx, dx);
+    s = __dadd_rn(s, __dmul_rn(dy, dy));
+    s = __dadd_rn(s, __dmul_rn(dz, dz));
+    return __dsqrt_rn(s) <= h;
+}
+
+// d2 of the pair in FP32; returns the reference's decision.
+__device__ __forceinline__ bool within(const float4& pi, const float4& pj, const SceneDev& sc,
+                                       float& dx, float& dy, float& dz, float& d2) {
+    dx = __fsub_rn(pi.x, pj.x);
+    dy = __fsub_rn(pi.y, pj.y);
+    dz = __fsub_rn(pi.z, pj.z);
+    d2 = __fmul_rn(dx, dx);
+    d2 = __fmaf_rn(dy, dy, d2);
+    d2 = __fmaf_rn(dz, dz, d2);
+    if (d2 < sc.h2_lo) return true;
+    if (d2 > sc.h2_hi) return false;
+    return within_exact(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, sc.h_d);
+}
+
+// ---- Kahan summation ------------------------------------------------------
+struct Kahan {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        float y = __fsub_rn(x, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
+// ---- the 27-voxel walk ----------------------------------------------------
+// Visits neighbours of a particle in the reference's order (voxel_kernels.py:
+// 46-61 dx outer, dy, dz inner; members in ascending particle id, which is
+// slot order inside a voxel) and stops after `cap` accepted neighbours
+// (self included, :77-84).  visit(j, dx, dy, dz, d2) is called per accepted
+// neighbour slot j.  Returns the number accepted.
+template <class Visit>
+__device__ __forceinline__ int walk(const float4 pi, const SceneDev& sc,
+                                    const int32_t* __restrict__ vstart,
+                                    const int32_t* __restrict__ vcount,
+                                    const float4* __restrict__ pos, int cap, Visit&& visit) {
+    const int cx = voxel_coord(pi.x, sc.vs[0], sc.dims[0]);
+    const int cy = voxel_coord(pi.y, sc.vs[1], sc.dims[1]);
+    const int cz = voxel_coord(pi.z, sc.vs[2], sc.dims[2]);
+    const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
+    // squared distances to the lower/upper faces of the own voxel, used to skip
+    // voxels that lie entirely beyond h (only when walk dims == table dims)
+    const float fx = pi.x - (float)cx * sc.vs[0];
+    const float fy = pi.y - (float)cy * sc.vs[1];
+    const float fz = pi.z - (float)cz * sc.vs[2];
+    const float gx0 = fx * fx, gx2 = (sc.vs[0] - fx) * (sc.vs[0] - fx);
+    const float gy0 = fy * fy, gy2 = (sc.vs[1] - fy) * (sc.vs[1] - fy);
+    const float gz0 = fz * fz, gz2 = (sc.vs[2] - fz) * (sc.vs[2] - fz);
+    const bool cull = !sc.walk_trunc;
+    int n = 0;
+#pragma unroll 1
+    for (int ddx = 0; ddx < 3; ++ddx) {
+        const int nx = cx + ddx - 1;
+        if (nx < 0 || nx >= w0) continue;
+        const float gx = ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f);
+#pragma unroll 1
+        for (int ddy = 0; ddy < 3; ++ddy) {
+            const int ny = cy + ddy - 1;
+            if (ny < 0 || ny >= w1) continue;
+            const float gxy = gx + (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
+#pragma unroll 1
+            for (int ddz = 0; ddz < 3; ++ddz) {
+                const int nz = cz + ddz - 1;
+                if (nz < 0 || nz >= w2) continue;
+                if (cull && gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > sc.cull2) continue;
+                const int vid = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
+                const int c = __ldg(vcount + vid);
+                if (c == 0) continue;
+                const int s0 = __ldg(vstart + vid);
+#pragma unroll 2
+                for (int m = 0; m < c; ++m) {
+                    const int j = s0 + m;
+                    const float4 pj = __ldg(pos + j);
+                    float dx, dy, dz, d2;
+                    if (within(pi, pj, sc, dx, dy, dz, d2)) {
+                        visit(j, dx, dy, dz, d2);
+                        if (++n >= cap) return n;
+                    }
+                }
+            }
+        }
+    }
+    return n;
+}
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw; SC 2011) -----------------
+__device__ __forceinline__ double philox_uniform(uint64_t seed, uint32_t pid, uint32_t step,
+                                                 uint32_t draw) {
+    uint32_t c0 = draw, c1 = step, c2 = pid, c3 = 0u;
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        if (r != 9) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    }
+    uint64_t bits = ((uint64_t)c0 << 21) | (c1 >> 11);
+    return (double)bits * (1.0 / 9007199254740992.0);
+}
+
+// ---- pipe geometry in FP64 (util_kernels.py) -------------------------------
+// pipe rows: [x0, y0, z0, r_start, length] (Pipe.to_numpy, data_classes.py:34-44)
+struct PipeView {
+    const double* p;
+    int rows;
+    __device__ __forceinline__ double at(int r, int c) const { return p[r * 5 + c]; }
+};
+
+// util_kernels.py:38-43
+__device__ inline double pipe_x_begin(const PipeView& P, int seg) {
+    double xb = P.at(0, 0);
+    for (int i = 0; i < seg; ++i) xb = __dadd_rn(xb, P.at(i, 4));
+    return xb;
+}
+
+// util_kernels.py:56-69
+__device__ inline double pipe_radius(const double* p, const PipeView& P, int seg) {
+    double r0 = P.at(seg, 3), r1 = P.at(seg + 1, 3), L = P.at(seg, 4);
+    if (r0 == r1) return r0;
+    if (r0 < r1) {
+        double delta = __dsub_rn(p[0], pipe_x_begin(P, seg));
+        double tl = __ddiv_rn(__dmul_rn(L, r0), __dsub_rn(r1, r0));
+        return __dmul_rn(r0, __dadd_rn(1.0, __ddiv_rn(delta, tl)));
+    }
+    double delta = __dsub_rn(__dadd_rn(pipe_x_begin(P, seg), L), p[0]);
+    double tl = __ddiv_rn(__dmul_rn(L, r1), __dsub_rn(r0, r1));
+    return __dmul_rn(r1, __dadd_rn(1.0, __ddiv_rn(delta, tl)));
+}
+
+// util_kernels.py:72-77
+__device__ inline int pipe_find_segment(const double* p, const PipeView& P) {
+    for (int j = 0; j < P.rows - 1; ++j)
+        if (P.at(j, 0) <= p[0] && p[0] < P.at(j + 1, 0)) return j;
+    return -1;
+}
+
+__device__ __forceinline__ double len3(const double* v) {
+    double l = __dmul_rn(v[0], v[0]);
+    l = __dadd_rn(l, __dmul_rn(v[1], v[1]));
+    l = __dadd_rn(l, __dmul_rn(v[2], v[2]));
+    return __dsqrt_rn(l);
+}
+
+__device__ __forceinline__ double dot3(const double* a, const double* b) {
+    double s = __dmul_rn(a[0], b[0]);
+    s = __dadd_rn(s, __dmul_rn(a[1], b[1]));
+    s = __dadd_rn(s, __dmul_rn(a[2], b[2]));
+    return s;
+}
+
+// util_kernels.py:46-53
+__device__ inline bool pipe_is_out(const double* p, const PipeView& P, int seg, double* radius) {
+    double yn = __dsub_rn(p[1], P.at(seg, 1)), zn = __dsub_rn(p[2], P.at(seg, 2));
+    double hh = __dsqrt_rn(__dadd_rn(__dmul_rn(yn, yn), __dmul_rn(zn, zn)));
+    double r = pipe_radius(p, P, seg);
+    if (radius) *radius = r;
+    return hh > r;
+}
+
+// solve_collision, util_kernels.py:182-204 with the helpers of :80-179
+__device__ inline void pipe_solve_collision(double* p, double* v, const PipeView& P, int seg) {
+    const double r0 = P.at(seg, 3), r1 = P.at(seg + 1, 3);
+    // calc_edge_vector :152-171
+    double yn = __dsub_rn(p[1], P.at(seg, 1)), zn = __dsub_rn(p[2], P.at(seg, 2));
+    double hh = __dsqrt_rn(__dadd_rn(__dmul_rn(yn, yn), __dmul_rn(zn, zn)));
+    double first[3], second[3], edge[3];
+    first[0] = P.at(seg, 0);
+    second[0] = P.at(seg + 1, 0);
+    for (int a = 1; a < 3; ++a) {
+        double q = __ddiv_rn(__dsub_rn(p[a], P.at(seg, a)), hh);
+        first[a] = __dmul_rn(q, r0);
+        second[a] = __dmul_rn(q, r1);
+    }
+    for (int a = 0; a < 3; ++a) edge[a] = __dsub_rn(second[a], first[a]);
+    for (int a = 1; a < 3; ++a) first[a] = __dadd_rn(first[a], P.at(seg, a));
+    // calc_collision_point :174-179, calc_dt :113-121, calc_distance_to_pipe :124-135
+    const double sl = len3(v), el = len3(edge);
+    const double cos_a = __ddiv_rn(dot3(v, edge), __dmul_rn(sl, el));
+    double pv[3], cr[3];
+    for (int a = 0; a < 3; ++a) pv[a] = __dsub_rn(first[a], p[a]);
+    cr[0] = __dsub_rn(__dmul_rn(edge[1], pv[2]), __dmul_rn(edge[2], pv[1]));
+    cr[1] = __dsub_rn(__dmul_rn(edge[2], pv[0]), __dmul_rn(edge[0], pv[2]));
+    cr[2] = __dsub_rn(__dmul_rn(edge[0], pv[1]), __dmul_rn(edge[1], pv[0]));
+    const double dd = __ddiv_rn(len3(cr), len3(edge));
+    const double sin_a = __dsqrt_rn(__dsub_rn(1.0, __dmul_rn(cos_a, cos_a)));
+    const double d_to = __ddiv_rn(dd, __dadd_rn(sin_a, 0.001));
+    const double dtc = __ddiv_rn(-d_to, sl);
+    double cp[3];
+    for (int a = 0; a < 3; ++a) cp[a] = __dadd_rn(p[a], __dmul_rn(v[a], dtc));
+    if (r0 == r1) {
+        v[1] = -v[1];
+        v[2] = -v[2];
+    } else {  // calc_summary_vector :88-94
+        const double ll = len3(edge), pl = len3(v);
+        const double c = __ddiv_rn(dot3(edge, v), __dmul_rn(ll, pl));
+        double sv[3];
+        for (int a = 0; a < 3; ++a)
+            sv[a] = __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(2.0, edge[a]), ll), c), pl);
+        for (int a = 0; a < 3; ++a) v[a] = __dsub_rn(sv[a], v[a]);
+    }
+    double w[3];
+    for (int a = 0; a < 3; ++a) w[a] = __dsub_rn(p[a], cp[a]);
+    const double way = len3(w);
+    const double svl = len3(v);
+    for (int a = 0; a < 3; ++a) p[a] = __dadd_rn(cp[a], __ddiv_rn(__dmul_rn(v[a], way), svl));
+}
+
+// collision_kernel (base_kernels.py:56-72) with put_particle_at_pipe_begin
+// (:101-113) and rand_position_inside_pipe (:116-127); respawn uniforms from
+// Philox keyed by (seed, particle id) with counter (draw, step).
+__device__ inline void pipe_collide(double* p, double* v, const PipeView& P, uint64_t seed,
+                                    uint32_t pid, uint32_t step) {
+    int seg = pipe_find_segment(p, P);
+    if (seg == -1) {
+        if (p[0] < 0.0) {
+            p[0] = -p[0];
+            v[0] = -v[0];
+            if (pipe_is_out(p, P, 0, nullptr)) pipe_solve_collision(p, v, P, 0);
+        } else {
+            p[0] = 0.0;
+            int s = pipe_find_segment(p, P);
+            if (s < 0) s = 0;  // a pipe starting after x = 0 (reference reads row -1)
+            double R = pipe_radius(p, P, s);
+            double r = __dmul_rn(R, __dsqrt_rn(philox_uniform(seed, pid, step, 0)));
+            double th = __dmul_rn(__dmul_rn(philox_uniform(seed, pid, step, 1), 2.0),
+                                  3.141592653589793);
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            p[1] = __dadd_rn(P.at(0, 1), __dmul_rn(r, cs));
+            p[2] = __dadd_rn(P.at(0, 2), __dmul_rn(r, sn));
+        }
+    } else if (pipe_is_out(p, P, seg, nullptr)) {
+        pipe_solve_collision(p, v, P, seg);
+    }
+}
+
+// ---- launchers (host) -----------------------------------------------------
+struct Launch {
+    const SceneDev* scenes;     // device array
+    const int32_t* pbegin;      // device, n_scenes + 1
+    int n_scenes;
+    int n;                      // particles (all scenes)
+    int v_total;                // voxels (all scenes)
+    const double* pipe;         // device pipe table (may be null)
+    cudaStream_t stream;
+};
+
+cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
+                              int32_t* vcount);
+cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
+                        int32_t* tile_sums, int n_tiles);
+int scan_tiles(int v_total);
+cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* slot,
+                           const int32_t* pid, const int32_t* vstart, int32_t* tmp_pid);
+cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
+                               const int32_t* tmp_pid, const int32_t* vstart,
+                               const int32_t* vcount, const float4* pos, const float4* vel,
+                               const double* pos64, float4* pos_out, float4* vel_out,
+                               int32_t* pid_out, double* pos64_out);
+cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
+                           const int32_t* vcount, float* rho, float2* aux);
+cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
+                          const float* rho, const float2* aux, const int32_t* vstart,
+                          const int32_t* vcount, float4* pressure, float4* viscosity);
+cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
+                             const float* rho, const float2* aux, const int32_t* pid,
+                             const double* pos64, const int32_t* vstart, const int32_t* vcount,
+                             const int32_t* scene_step, float4* pos_out, float4* vel_out,
+                             int32_t* pid_out, double* pos64_out, float4* force_out);
+cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
+                              const int32_t* vcount, int32_t* list, int stride,
+                              int32_t* n_capped, int32_t* n_uncapped);
+cudaError_t launch_aux_from_rho(const Launch& L, const float* rho, float2* aux);
+
+}  // namespace sphgb

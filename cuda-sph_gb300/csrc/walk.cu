@@ -1,0 +1,258 @@
+// walk.cu -- neighbour walk kernels: density, forces, fused force + integrate +
+// wall response, and the neighbour list/count kernel used for parity.
+//
+// One thread per particle in voxel-sorted order, so that the threads of a
+// block walk overlapping voxel neighbourhoods and their candidate loads are
+// served from L1.  The walk order and the 32-neighbour cap are the reference's
+// (get_neighbours, sim/src/sph/kernels/voxel_kernels.py:30-85).
+#include "sphgb_internal.cuh"
+
+namespace sphgb {
+
+namespace {
+
+inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
+
+// density_kernel, voxel_kernels.py:109-132: rho_i = MASS * sum_{j != i} W_ij,
+// W = W_CONST (h^2 - r^2)^3 (base_kernels.py:6-9), written here as
+// W_CONST h^6 (1 - r^2/h^2)^3 so the FP32 sum stays in range for any h.
+// Also writes aux_i = (p_i / rho_i^2, 1 / rho_i) with p = K (rho - RHO_0), the
+// per-particle factors of the force pass (voxel_kernels.py:162-164, :205-208).
+__global__ void __launch_bounds__(kBlock)
+k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+          int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
+          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const float4 pi = __ldg(pos + s);
+    const float inv_h2 = 1.0f / sc.h2;
+    Kahan acc;
+    walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float, float, float, float d2) {
+        if (j != s) {
+            const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+            acc.add(u * u * u);
+        }
+    });
+    const float r = (acc.s * sc.w_const) * sc.mass;
+    rho[s] = r;
+    if (aux) {
+        const float p = sc.k * (r - sc.rho0);
+        aux[s] = make_float2(p / (r * r), 1.0f / r);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_aux(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+      int n, const float* __restrict__ rho, float2* __restrict__ aux) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const float r = rho[s];
+    const float p = sc.k * (r - sc.rho0);
+    aux[s] = make_float2(p / (r * r), 1.0f / r);
+}
+
+struct ForceSums {
+    Kahan px, py, pz, vx, vy, vz;
+};
+
+// pressure_kernel (voxel_kernels.py:136-171) and viscosity_kernel (:175-211)
+// for one particle, same neighbour set as the density pass.
+//   P_i = sum_j (p_i/rho_i^2 + p_j/rho_j^2) grad W_ij,
+//         grad W = GRAD_W_CONST (h - r)^2 (x_i - x_j) / r   (base_kernels.py:12-21)
+//   V_i = min(1, sum_j MASS VISC (v_j - v_i) / rho_j lap W_ij / rho_i),
+//         lap W = LAP_W_CONST (h - r)                        (base_kernels.py:24-27)
+// with (h - r) written as h (1 - r/h).
+__device__ __forceinline__ void force_sums(int s, const float4& pi, const float4& vi,
+                                           float a_i, const SceneDev& sc,
+                                           const float4* __restrict__ pos,
+                                           const float4* __restrict__ vel,
+                                           const float2* __restrict__ aux,
+                                           const int32_t* __restrict__ vstart,
+                                           const int32_t* __restrict__ vcount, ForceSums& f) {
+    const float inv_h = 1.0f / sc.h;
+    walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float dx, float dy, float dz, float d2) {
+        if (j == s) return;
+        const float2 aj = __ldg(aux + j);
+        const float4 vj = __ldg(vel + j);
+        const float r = sqrtf(d2);
+        const float inv_r = 1.0f / r;
+        const float t = __fmaf_rn(-r, inv_h, 1.0f);
+        const float g = ((a_i + aj.x) * sc.grad_w_const) * (t * t) * inv_r;
+        f.px.add(g * dx);
+        f.py.add(g * dy);
+        f.pz.add(g * dz);
+        const float l = (sc.lap_w_const * t) * aj.y;
+        f.vx.add(l * (vj.x - vi.x));
+        f.vy.add(l * (vj.y - vi.y));
+        f.vz.add(l * (vj.z - vi.z));
+    });
+}
+
+__device__ __forceinline__ float clamp1(float x) { return x < 1.0f ? x : 1.0f; }  // min(1, x)
+
+__global__ void __launch_bounds__(kBlock)
+k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+         int n, const float4* __restrict__ pos, const float4* __restrict__ vel,
+         const float2* __restrict__ aux, const int32_t* __restrict__ vstart,
+         const int32_t* __restrict__ vcount, float4* __restrict__ pressure,
+         float4* __restrict__ viscosity) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const float4 pi = __ldg(pos + s);
+    const float4 vi = __ldg(vel + s);
+    const float2 ai = __ldg(aux + s);
+    ForceSums f;
+    force_sums(s, pi, vi, ai.x, sc, pos, vel, aux, vstart, vcount, f);
+    const float vscale = sc.mass * sc.visc * ai.y;
+    pressure[s] = make_float4(f.px.s, f.py.s, f.pz.s, 0.0f);
+    viscosity[s] = make_float4(clamp1(f.vx.s * vscale), clamp1(f.vy.s * vscale),
+                               clamp1(f.vz.s * vscale), 0.0f);
+}
+
+// forces + integrating_kernel (base_kernels.py:30-53) + wall response
+// (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
+// state into the *_out buffers at the same slot.
+__global__ void __launch_bounds__(kBlock)
+k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+            int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
+            const float4* __restrict__ vel, const float* __restrict__ rho,
+            const float2* __restrict__ aux, const int32_t* __restrict__ pid,
+            const double* __restrict__ pos64, const int32_t* __restrict__ vstart,
+            const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
+            float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+            int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
+            float4* __restrict__ force_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int si = scene_of(s, pbegin, n_scenes);
+    const SceneDev& sc = scenes[si];
+    const float4 pi = __ldg(pos + s);
+    const float4 vi = __ldg(vel + s);
+    const float2 ai = __ldg(aux + s);
+    const float rho_i = __ldg(rho + s);
+    ForceSums f;
+    force_sums(s, pi, vi, ai.x, sc, pos, vel, aux, vstart, vcount, f);
+    const float vscale = sc.mass * sc.visc * ai.y;
+    // result_force = ext + -P + V (base_kernels.py:46-52)
+    float F[3];
+    F[0] = (sc.ext[0] + -f.px.s) + clamp1(f.vx.s * vscale);
+    F[1] = (sc.ext[1] + -f.py.s) + clamp1(f.vy.s * vscale);
+    F[2] = (sc.ext[2] + -f.pz.s) + clamp1(f.vz.s * vscale);
+    float v[3] = {vi.x, vi.y, vi.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
+    const int p_id = __ldg(pid + s);
+    if (sc.mode == 0) {
+        float x[3] = {pi.x, pi.y, pi.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            x[a] = x[a] + v[a] * sc.dt;
+            bool bounced = false;
+            if (x[a] < 0.0f) { x[a] = sc.wall_lo; bounced = true; }
+            if (x[a] > sc.space[a]) { x[a] = sc.wall_hi[a]; bounced = true; }
+            if (bounced) v[a] = -v[a] * sc.damp;
+        }
+        pos_out[s] = make_float4(x[0], x[1], x[2], 0.0f);
+        if (pos64_out) {
+            pos64_out[3 * s + 0] = x[0];
+            pos64_out[3 * s + 1] = x[1];
+            pos64_out[3 * s + 2] = x[2];
+        }
+    } else {
+        // pipe flow: FP64 position accumulator and FP64 wall response
+        double x[3], vd[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            vd[a] = (double)v[a];
+            x[a] = __dadd_rn(pos64[3 * s + a], __dmul_rn(vd[a], sc.dt_d));
+        }
+        PipeView P{pipe + 5 * sc.pipe_off, sc.pipe_rows};
+        pipe_collide(x, vd, P, sc.seed, (uint32_t)p_id, (uint32_t)__ldg(scene_step + si));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            v[a] = (float)vd[a];
+            pos64_out[3 * s + a] = x[a];
+        }
+        pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
+    }
+    vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
+    pid_out[s] = p_id;
+    if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_neighbours(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+             int n_scenes, int n, const float4* __restrict__ pos,
+             const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+             int32_t* __restrict__ list, int stride, int32_t* __restrict__ n_capped,
+             int32_t* __restrict__ n_uncapped) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const float4 pi = __ldg(pos + s);
+    int k = 0;
+    int32_t* li = list ? list + (size_t)s * stride : nullptr;
+    const int c = walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float, float, float, float) {
+        if (li && k < stride) li[k] = j;
+        ++k;
+    });
+    if (li) for (int t = c; t < stride; ++t) li[t] = -1;
+    if (n_capped) n_capped[s] = c;
+    if (n_uncapped)
+        n_uncapped[s] = walk(pi, sc, vstart, vcount, pos, 0x7fffffff,
+                             [&](int, float, float, float, float) {});
+}
+
+}  // namespace
+
+cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
+                           const int32_t* vcount, float* rho, float2* aux) {
+    if (L.n == 0) return cudaSuccess;
+    k_density<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
+                                                         vstart, vcount, rho, aux);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aux_from_rho(const Launch& L, const float* rho, float2* aux) {
+    if (L.n == 0) return cudaSuccess;
+    k_aux<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, rho, aux);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
+                          const float* rho, const float2* aux, const int32_t* vstart,
+                          const int32_t* vcount, float4* pressure, float4* viscosity) {
+    (void)rho;
+    if (L.n == 0) return cudaSuccess;
+    k_forces<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
+                                                        vel, aux, vstart, vcount, pressure,
+                                                        viscosity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
+                             const float* rho, const float2* aux, const int32_t* pid,
+                             const double* pos64, const int32_t* vstart, const int32_t* vcount,
+                             const int32_t* scene_step, float4* pos_out, float4* vel_out,
+                             int32_t* pid_out, double* pos64_out, float4* force_out) {
+    if (L.n == 0) return cudaSuccess;
+    k_integrate<<<blocks_for(L.n), kBlock, 0, L.stream>>>(
+        L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
+        vcount, scene_step, pos_out, vel_out, pid_out, pos64_out, force_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
+                              const int32_t* vcount, int32_t* list, int stride,
+                              int32_t* n_capped, int32_t* n_uncapped) {
+    if (L.n == 0) return cudaSuccess;
+    k_neighbours<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n,
+                                                            pos, vstart, vcount, list, stride,
+                                                            n_capped, n_uncapped);
+    return cudaGetLastError();
+}
+
+}  // namespace sphgb

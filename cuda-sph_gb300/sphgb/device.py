@@ -1,0 +1,216 @@
+"""Device-resident scenes: the state of one or more independent scenes kept in
+HBM and advanced by libsphgb.so.
+
+Layout on the device (FP32 unless noted), for N particles over all scenes:
+  pos   (N, 4)  x, y, z, unused        -- voxel-sorted slot order
+  vel   (N, 4)  vx, vy, vz, unused
+  rho   (N,)    density of the last step (computed from its start positions)
+  pid   (N,)    int32 particle id within its scene at each slot
+  pos64 (N, 3)  FP64 position accumulator (allocated when a scene is a pipe)
+  steps (S,)    int32 steps taken per scene (keys the respawn random stream)
+Scenes occupy consecutive slot ranges in the order given.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence
+
+import ctypes as C
+import numpy as np
+
+from . import _capi
+from .config import SPHConstants, f32
+from .data_classes import SimulationParameters, SimulationState
+
+
+@dataclass
+class SceneSpec:
+    """One scene: the reference's SimulationParameters plus its constants and
+    enclosure mode ('BOX' or 'PIPE', the reference's config.SIM_MODE)."""
+    params: SimulationParameters
+    constants: SPHConstants = field(default_factory=SPHConstants)
+    mode: str = 'BOX'
+
+    @property
+    def n(self) -> int:
+        return int(self.params.particle_count)
+
+
+def scene_params(spec: SceneSpec, pipe_row_offset: int = 0) -> _capi.SceneParams:
+    """SphgbSceneParams for a scene, every value rounded to FP32 first."""
+    p, c = spec.params, spec.constants.rounded()
+    sp = _capi.SceneParams()
+    sp.particle_count = int(p.particle_count)
+    space = f32(np.asarray(p.space_size, dtype=np.float64))
+    voxel = f32(np.asarray(p.voxel_size, dtype=np.float64))
+    ext = f32(np.asarray(p.external_force, dtype=np.float64))
+    for a in range(3):
+        sp.space_size[a] = float(space[a])
+        sp.voxel_size[a] = float(voxel[a])
+        sp.external_force[a] = float(ext[a])
+    sp.dt = float(f32(1.0 / float(p.fps)))
+    sp.mass, sp.rho_0, sp.inf_r = c.mass, c.rho_0, c.inf_r
+    sp.visc, sp.k, sp.damp = c.visc, c.k, c.damp
+    sp.max_neighbours = int(c.max_neighbours)
+    if spec.mode not in ('BOX', 'PIPE'):
+        raise Exception(f'Wrong simulation mode! ({spec.mode})')
+    sp.mode = _capi.MODE_PIPE if spec.mode == 'PIPE' else _capi.MODE_BOX
+    if c.walk_dims not in ('ceil', 'truncated'):
+        raise ValueError(f"walk_dims must be 'ceil' or 'truncated', not {c.walk_dims!r}")
+    sp.walk_dims = _capi.WALK_TRUNCATED if c.walk_dims == 'truncated' else _capi.WALK_CEIL
+    sp.pipe_rows = len(p.pipe.to_numpy()) if spec.mode == 'PIPE' else 0
+    sp.pipe_row_offset = pipe_row_offset if spec.mode == 'PIPE' else 0
+    sp.seed = int(c.seed)
+    return sp
+
+
+class SceneBatch:
+    """Scenes resident on one GPU, advanced together by one launch sequence."""
+
+    def __init__(self, specs: Sequence[SceneSpec], device: str = "cuda"):
+        import torch
+        self._torch = torch
+        self.specs: List[SceneSpec] = list(specs)
+        if not self.specs:
+            raise ValueError("need at least one scene")
+        self.device = torch.device(device)
+        lib = _capi.load()
+        rows, params = [], []
+        for s in self.specs:
+            params.append(scene_params(s, pipe_row_offset=len(rows)))
+            if s.mode == 'PIPE':
+                rows.extend(np.asarray(s.params.pipe.to_numpy(), dtype=np.float64))
+        self.pipe_table = (np.ascontiguousarray(np.stack(rows), dtype=np.float64)
+                           if rows else np.zeros((0, 5)))
+        arr = (_capi.SceneParams * len(params))(*params)
+        self._params = arr
+        handle = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _capi.check(lib.sphgb_ctx_create(arr, len(params),
+                                             self.pipe_table.ctypes.data if rows else None,
+                                             len(rows), C.byref(handle)), "sphgb_ctx_create")
+        self._ctx = handle
+        n = C.c_int64()
+        v = C.c_int64()
+        _capi.check(lib.sphgb_ctx_sizes(self._ctx, C.byref(n), C.byref(v)), "sphgb_ctx_sizes")
+        self.n, self.n_voxels = int(n.value), int(v.value)
+        self.scene_sizes = [s.n for s in self.specs]
+        self.scene_offsets = list(np.concatenate([[0], np.cumsum(self.scene_sizes)[:-1]]).astype(int))
+        self.any_pipe = any(s.mode == 'PIPE' for s in self.specs)
+        dev = self.device
+        self.pos = torch.zeros((max(self.n, 1), 4), dtype=torch.float32, device=dev)
+        self.vel = torch.zeros((max(self.n, 1), 4), dtype=torch.float32, device=dev)
+        self.rho = torch.zeros((max(self.n, 1),), dtype=torch.float32, device=dev)
+        self.pid = torch.zeros((max(self.n, 1),), dtype=torch.int32, device=dev)
+        self.pos64 = torch.zeros((max(self.n, 1) if self.any_pipe else 1, 3),
+                                 dtype=torch.float64, device=dev)
+        self.steps = torch.zeros((len(self.specs),), dtype=torch.int32, device=dev)
+        _capi.check(lib.sphgb_ctx_bind_state(
+            self._ctx, self.pos.data_ptr(), self.vel.data_ptr(), self.rho.data_ptr(),
+            self.pid.data_ptr(), self.pos64.data_ptr(), self.steps.data_ptr()),
+            "sphgb_ctx_bind_state")
+
+    # -- helpers ---------------------------------------------------------
+    def _stream(self, stream=None) -> int:
+        torch = self._torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        return s.cuda_stream
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            _capi.load().sphgb_ctx_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state in / out --------------------------------------------------
+    def load_states(self, states: Sequence[SimulationState], stream=None) -> None:
+        """Upload host states (SimulationState per scene, original particle order)."""
+        torch = self._torch
+        if len(states) != len(self.specs):
+            raise ValueError("one state per scene")
+        pos = np.concatenate([np.asarray(s.position, dtype=np.float64).reshape(-1, 3)
+                              for s in states])
+        vel = np.concatenate([np.asarray(s.velocity, dtype=np.float64).reshape(-1, 3)
+                              for s in states])
+        if len(pos) != self.n or len(vel) != self.n:
+            raise ValueError("state sizes do not match the scenes' particle counts")
+        self.load_aos_device(torch.from_numpy(np.ascontiguousarray(pos)).to(self.device),
+                             torch.from_numpy(np.ascontiguousarray(vel)).to(self.device), stream)
+
+    def load_aos_device(self, pos_aos, vel_aos, stream=None) -> None:
+        """Load FP64 (N, 3) device tensors in original order (scene-concatenated)."""
+        _capi.call("sphgb_ctx_load_aos_f64", self._ctx, pos_aos.data_ptr(), vel_aos.data_ptr(),
+                   self._stream(stream))
+        self.steps.zero_()
+
+    def export_aos_f64(self, stream=None):
+        """(pos, vel, rho) as FP64 device tensors in original particle order."""
+        torch = self._torch
+        n = max(self.n, 1)
+        pos = torch.empty((n, 3), dtype=torch.float64, device=self.device)
+        vel = torch.empty((n, 3), dtype=torch.float64, device=self.device)
+        rho = torch.empty((n,), dtype=torch.float64, device=self.device)
+        _capi.call("sphgb_ctx_store_aos_f64", self._ctx, pos.data_ptr(), vel.data_ptr(),
+                   rho.data_ptr(), self._stream(stream))
+        return pos[:self.n], vel[:self.n], rho[:self.n]
+
+    def states(self) -> List[SimulationState]:
+        pos, vel, rho = (t.cpu().numpy() for t in self.export_aos_f64())
+        out = []
+        for off, n in zip(self.scene_offsets, self.scene_sizes):
+            out.append(SimulationState(pos[off:off + n].copy(), vel[off:off + n].copy(),
+                                       rho[off:off + n].copy()))
+        return out
+
+    # -- stepping and diagnostics ----------------------------------------
+    def step(self, n_steps: int = 1, use_graph: bool = False, stream=None) -> None:
+        _capi.call("sphgb_ctx_step", self._ctx, int(n_steps), 1 if use_graph else 0,
+                   self._stream(stream))
+
+    STAGES = ("hash", "scan", "scatter", "rank_gather", "density", "force_integrate",
+              "step_counter")
+
+    def step_profiled(self, n_steps: int = 1, stream=None) -> dict:
+        """Step without a graph, timing every stage with CUDA events on the
+        launching stream; returns mean milliseconds per step per stage."""
+        out = (C.c_float * len(self.STAGES))()
+        _capi.call("sphgb_ctx_step_profiled", self._ctx, int(n_steps), self._stream(stream), out)
+        return dict(zip(self.STAGES, [float(v) for v in out]))
+
+    def conservation(self, stream=None) -> np.ndarray:
+        """(S, 8) FP64: mass, momentum xyz, kinetic, potential, total energy, particles."""
+        torch = self._torch
+        out = torch.zeros((len(self.specs), 8), dtype=torch.float64, device=self.device)
+        _capi.call("sphgb_ctx_conservation", self._ctx, out.data_ptr(), self._stream(stream))
+        return out.cpu().numpy()
+
+    def neighbour_counts(self, stream=None):
+        """(capped, uncapped) neighbour counts per particle, original order."""
+        torch = self._torch
+        n = max(self.n, 1)
+        cap = torch.zeros((n,), dtype=torch.int32, device=self.device)
+        unc = torch.zeros((n,), dtype=torch.int32, device=self.device)
+        _capi.call("sphgb_ctx_neighbour_counts", self._ctx, cap.data_ptr(), unc.data_ptr(),
+                   self._stream(stream))
+        return cap[:self.n].cpu().numpy(), unc[:self.n].cpu().numpy()
+
+    def compute_next_state_host(self, pos, vel, pos_out=None, vel_out=None, rho_out=None):
+        """One step through the host-buffer entry point (one-scene batches)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        n = self.n
+        pos_out = np.empty((n, 3)) if pos_out is None else pos_out
+        vel_out = np.empty((n, 3)) if vel_out is None else vel_out
+        rho_out = np.empty((n,)) if rho_out is None else rho_out
+        _capi.call("sphgb_compute_next_state_host", self._ctx, pos.ctypes.data, vel.ctypes.data,
+                   pos_out.ctypes.data, vel_out.ctypes.data, rho_out.ctypes.data)
+        return pos_out, vel_out, rho_out

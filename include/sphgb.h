@@ -1,0 +1,221 @@
+/*
+ * sphgb.h -- C ABI of the GB300 (sm_103a) SPH step library, libsphgb.so.
+ *
+ * The library replaces the per-step path of iwoplaza/cuda-sph's voxel strategy,
+ * VoxelSPHStrategy.compute_next_state (sim/src/sph/strategies/
+ * abstract_sph_strategy.py:31-46 with voxel_sph_strategy.py:20-116): voxel hash,
+ * voxel sort and voxel_begin table, the 27-voxel neighbour walk, density,
+ * pressure and viscosity terms, integration and the box or pipe wall response.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: SPHGB_OK (0) or a negative
+ *    SPHGB_ERR_*; sphgb_last_error() returns a message for the calling thread.
+ *    No C++ exception crosses this boundary.
+ *  - Pointers named d_* are device pointers, h_* host pointers.  The library
+ *    never frees caller memory.  Scratch buffers are owned by a context.
+ *  - `stream` is a cudaStream_t passed as void* (0 = legacy default stream).
+ *    Work is enqueued asynchronously unless the entry point says otherwise.
+ *  - A context is not thread-safe; use one context per host thread.
+ *  - Particle state on the device is FP32: position and velocity as float4
+ *    (x, y, z, unused) per particle, density as float, particle ids as int32.
+ *    Device state is kept in voxel-sorted order; d_pid[s] names the original
+ *    particle at sorted slot s.
+ */
+#ifndef SPHGB_H
+#define SPHGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHGB_ABI_VERSION 1
+
+enum {
+    SPHGB_OK = 0,
+    SPHGB_ERR_INVALID = -1,   /* bad argument (null pointer, size, mode) */
+    SPHGB_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+    SPHGB_ERR_NOMEM = -3,     /* device allocation failed */
+    SPHGB_ERR_STATE = -4,     /* call out of order (e.g. step before bind) */
+    SPHGB_ERR_RANGE = -5      /* a size is beyond a documented limit */
+};
+
+enum { SPHGB_MODE_BOX = 0, SPHGB_MODE_PIPE = 1 };      /* config.SIM_MODE (config.py:13) */
+enum { SPHGB_WALK_CEIL = 0, SPHGB_WALK_TRUNCATED = 1 }; /* see walk_dims below */
+
+/*
+ * One scene: SimulationParameters (common/data_classes.py:70-78) plus the
+ * physics constants the reference freezes from config.py:18-30 at JIT time.
+ * Doubles are rounded to FP32 on the device; pass FP32-representable values for
+ * bit-comparable results against an FP64 implementation.
+ */
+typedef struct SphgbSceneParams {
+    int64_t particle_count;    /* SimulationParameters.particle_count */
+    double space_size[3];      /* SimulationParameters.space_size (box extent) */
+    double voxel_size[3];      /* SimulationParameters.voxel_size */
+    double external_force[3];  /* SimulationParameters.external_force */
+    double dt;                 /* 1 / fps (abstract_sph_strategy.py:20) */
+    double mass;               /* MASS   (config.py:18) */
+    double rho_0;              /* RHO_0  (config.py:19) */
+    double inf_r;              /* INF_R  (config.py:20), the smoothing radius h */
+    double visc;               /* VISC   (config.py:21) */
+    double k;                  /* K      (config.py:22), gas constant */
+    double damp;               /* DAMP   (config.py:23), wall restitution */
+    int32_t max_neighbours;    /* MAX_NEIGHBOURS (config.py:30); <= 0 means no cap */
+    int32_t mode;              /* SPHGB_MODE_BOX or SPHGB_MODE_PIPE */
+    /* Voxel dims used by the neighbour walk.  The voxel table always uses
+     * ceil(space/voxel) (voxel_sph_strategy.py:70-73).  SPHGB_WALK_CEIL walks
+     * with the same dims.  SPHGB_WALK_TRUNCATED reproduces the reference's
+     * walk exactly: it builds neighbour voxel ids with int(space/voxel)
+     * (voxel_sph_strategy.py:110-116), which differ from the table's dims when
+     * space is not a multiple of the voxel size. */
+    int32_t walk_dims;
+    int32_t pipe_rows;         /* rows of Pipe.to_numpy() (segments + 1); 0 in box mode */
+    int64_t pipe_row_offset;   /* first row of this scene in the pipe table */
+    uint64_t seed;             /* respawn random stream key (abstract_sph_strategy.py:27) */
+} SphgbSceneParams;
+
+#ifndef SPHGB_NO_FUNCTIONS
+
+typedef struct SphgbCtx SphgbCtx;
+
+/* ---- library ---------------------------------------------------------- */
+int sphgb_abi_version(void);
+/* sizeof(SphgbSceneParams), for binding checks. */
+int sphgb_scene_params_size(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* sphgb_last_error(void);
+
+/* ---- context ----------------------------------------------------------
+ * A context advances one or more independent scenes together.  With one
+ * scene it is the reference's strategy object (AbstractSPHStrategy.__init__,
+ * abstract_sph_strategy.py:18-29); with many it is the batched path.
+ * pipe_rows_table: host doubles [total rows][5] in Pipe.to_numpy() layout
+ * (common/data_classes.py:34-44); may be NULL when no scene is in pipe mode.
+ * Allocates all scratch with cudaMalloc on the current device. */
+int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes,
+                     const double* pipe_rows_table, int n_pipe_rows_total,
+                     SphgbCtx** out_ctx);
+int sphgb_ctx_destroy(SphgbCtx* ctx);
+/* Total particles / voxels over all scenes of the context. */
+int sphgb_ctx_sizes(const SphgbCtx* ctx, int64_t* n_particles, int64_t* n_voxels);
+
+/* Bind caller-owned device state (voxel-sorted order, see conventions).
+ * d_pos64 (3 doubles per particle) is required when any scene is in pipe mode
+ * (FP64 position accumulator) and ignored otherwise.  d_scene_step: one int32
+ * per scene, the number of steps each scene has taken. */
+int sphgb_ctx_bind_state(SphgbCtx* ctx, float* d_pos, float* d_vel, float* d_rho,
+                         int32_t* d_pid, double* d_pos64, int32_t* d_scene_step);
+
+/* Load state from FP64 AoS arrays in original particle order (the layout of
+ * SimulationState.position / .velocity, common/data_classes.py:81-85) already
+ * on the device; sets pid = identity and the FP64 accumulator. */
+int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double* d_vel_aos,
+                           void* stream);
+/* Write the bound state back as FP64 AoS in original particle order. */
+int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
+                            double* d_rho, void* stream);
+
+/* Advance every scene n_steps steps (compute_next_state, repeated) on the
+ * bound state.  With use_graph != 0 the n_steps sequence is captured once
+ * into a CUDA graph and replayed on later calls with the same n_steps. */
+int sphgb_ctx_step(SphgbCtx* ctx, int n_steps, int use_graph, void* stream);
+
+/* Advance n_steps steps without a graph, with a CUDA event after every
+ * stage; synchronises the stream and writes the mean milliseconds per step of
+ * each stage to h_stage_ms[SPHGB_PROFILE_STAGES]:
+ * [hash+histogram (with the histogram clear), scan, scatter, rank-gather,
+ *  density, force+integrate+wall, step counter]. */
+#define SPHGB_PROFILE_STAGES 7
+int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_stage_ms);
+
+/* The reference's boundary with host buffers: FP64 AoS state in, next FP64
+ * AoS state out, synchronous (AbstractSPHStrategy.compute_next_state,
+ * abstract_sph_strategy.py:31-46, including its host<->device copies at
+ * :65-74 and :77-84).  Context must hold exactly one scene.  Host buffers may
+ * be pageable or pinned (pinned is faster). */
+int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
+                                  double* h_pos_out, double* h_vel_out, double* h_rho_out);
+
+/* Per-scene conservation sums in FP64, fixed summation order (identical for a
+ * scene whether it runs alone or batched).  d_out: 8 doubles per scene:
+ * [mass, px, py, pz, kinetic, potential, kinetic + potential, particles].
+ * Potential energy is -m g.x with g = external_force. */
+int sphgb_ctx_conservation(SphgbCtx* ctx, double* d_out, void* stream);
+
+/* Neighbour statistics of the bound state at its current positions: capped
+ * and uncapped neighbour counts (self included) per particle, in original
+ * particle order (scene-concatenated).  Uses the context's scratch buffers. */
+int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_uncapped,
+                               void* stream);
+
+/* ---- stages (each launches the same kernels sphgb_ctx_step uses) ------- */
+
+/* assign_voxels_to_particles_kernel (voxel_kernels.py:89-105): voxel id of
+ * each particle (ceil dims; coordinates clamped to the table). */
+int sphgb_assign_voxels(SphgbCtx* ctx, const float* d_pos, int32_t* d_voxel_out, void* stream);
+
+/* Voxel sort + voxel_begin (voxel_sph_strategy.py:65-107): stable counting
+ * sort by (voxel id, particle id).  Reads state (d_pos, d_vel, d_pid) in any
+ * order, writes it voxel-sorted to the *_out buffers, and writes the voxel
+ * table: d_voxel_start[v] (first sorted slot) and d_voxel_count[v]. */
+int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
+                          const int32_t* d_pid, const double* d_pos64,
+                          float* d_pos_out, float* d_vel_out, int32_t* d_pid_out,
+                          double* d_pos64_out, int32_t* d_voxel_start,
+                          int32_t* d_voxel_count, void* stream);
+
+/* get_neighbours (voxel_kernels.py:30-85) for every sorted slot: the ordered,
+ * capped neighbour list (sorted slots, -1 padded; d_list may be NULL) with
+ * list_stride entries per particle, and the capped/uncapped counts. */
+int sphgb_neighbours(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_voxel_start,
+                     const int32_t* d_voxel_count, int32_t* d_list, int list_stride,
+                     int32_t* d_count_capped, int32_t* d_count_uncapped, void* stream);
+
+/* density_kernel (voxel_kernels.py:109-132) on sorted state. */
+int sphgb_density(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_voxel_start,
+                  const int32_t* d_voxel_count, float* d_rho_out, void* stream);
+
+/* pressure_kernel + viscosity_kernel (voxel_kernels.py:136-211) on sorted
+ * state: pressure and viscosity terms as float4 per particle. */
+int sphgb_forces(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_sorted,
+                 const float* d_rho_sorted, const int32_t* d_voxel_start,
+                 const int32_t* d_voxel_count, float* d_pressure_out,
+                 float* d_viscosity_out, void* stream);
+
+/* Forces fused with integrating_kernel (base_kernels.py:30-53) and the wall
+ * response (collision_kernel_box :75-98 or collision_kernel :56-72): reads
+ * sorted state, writes the next state (same slot order) to the *_out buffers
+ * and, if d_force_out is not NULL, result_force as float4.  step_index keys
+ * the respawn random stream. */
+int sphgb_integrate(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_sorted,
+                    const float* d_rho_sorted, const int32_t* d_pid_sorted,
+                    const double* d_pos64_sorted, const int32_t* d_voxel_start,
+                    const int32_t* d_voxel_count, const int32_t* d_scene_step,
+                    float* d_pos_out, float* d_vel_out, int32_t* d_pid_out,
+                    double* d_pos64_out, float* d_force_out, void* stream);
+
+/* ---- pipe geometry (sim/src/sph/kernels/util_kernels.py), FP64 --------
+ * Batch wrappers over the device functions the pipe wall response uses, for
+ * the reference's known-answer tests (sim/tests/test_collisions.py). */
+int sphgb_pipe_find_segment(const double* d_pos, int n, const double* d_pipe, int pipe_rows,
+                            int32_t* d_seg_out, void* stream);
+int sphgb_pipe_is_out(const double* d_pos, const int32_t* d_seg, int n, const double* d_pipe,
+                      int pipe_rows, int32_t* d_out, double* d_radius_out, void* stream);
+int sphgb_pipe_x_at_segment_beginning(const int32_t* d_seg, int n, const double* d_pipe,
+                                      int pipe_rows, double* d_out, void* stream);
+/* In place: for each particle, find_segment; if out of the pipe, solve_collision. */
+int sphgb_pipe_solve_collision(double* d_pos, double* d_vel, int n, const double* d_pipe,
+                               int pipe_rows, int32_t* d_seg_out, void* stream);
+/* Philox4x32-10 uniforms in [0,1) for (seed, pid, step, draw) -- the respawn stream. */
+int sphgb_philox_uniform(uint64_t seed, const int32_t* d_pid, int n, int step, int draw,
+                         double* d_out, void* stream);
+
+#endif /* SPHGB_NO_FUNCTIONS */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPHGB_H */
