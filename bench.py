@@ -10,7 +10,13 @@ larger than the 129 MB L2, so no flush is needed between steps.
 
 --impl gb300 (default): W untimed steps, then K steps timed with CUDA events
 (one CUDA-graph replay per step), barrier + synchronize on both sides, max over
-ranks.  Under torchrun each rank advances its own replica of the scene (the
+ranks.  Every step is a complete compute_next_state of the same resident
+input (the dam-break start state), written to separate output buffers: under
+the reference's formulas this scene is not stable (the pressure term has no
+MASS factor, voxel_kernels.py:171, so forces scale like h^-4; the FP64 oracle
+reaches |v| = 571 m/s at step 2 and non-finite velocities at step 3), so a
+free-running benchmark would time the collapse instead of the step.  The
+free-running rate over the first steps is reported beside it.  Under torchrun each rank advances its own replica of the scene (the
 single scene does not shard; replicas only).  Also reported:
   e2e      the same metric through the C ABI host-buffer entry point
            (sphgb_compute_next_state_host): FP64 AoS state copied from pinned
@@ -46,13 +52,21 @@ STAGE_BYTES_PER_VOXEL = {"hash": 4, "scan": 8}
 KERNELS_PER_STEP = 9   # hash, 3 scan, scatter, rank-gather, density, force+integrate, counter
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line alone goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.2f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["config2", "config0"], default="config2")
+    ap.add_argument("--workload", choices=["config2", "box2m", "config0"], default="config2")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=2, help="oracle steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -66,6 +80,12 @@ def workload(name):
         desc = ("4M-particle dam-break box: 128x256x128 jittered lattice, spacing 0.005, "
                 "box [0,2]^3, h 0.0112, mass 1.25e-4, rho0 1000, K 3, visc 3.5, g -9.81, "
                 "restitution 0.5, dt 5e-4, 32-neighbour cap")
+    elif name == "box2m":
+        # profiling case: same spacing, h and box as the 4M scene, 2M particles
+        # (kernel inputs still above the 129 MB L2)
+        spec, st = scenes.box_dam_break(nx=100, ny=200, nz=100, spacing=0.005, jitter=0.0005,
+                                        box=(2.0, 2.0, 2.0), h=0.0112, mass=1.25e-4, seed=2)
+        desc = "2M-particle dam-break box (100x200x100 lattice, spacing 0.005, h 0.0112, [0,2]^3)"
     else:
         spec, st = scenes.config0()
         desc = "8k-particle dam-break box (16x32x16 lattice, h 0.045), 32-neighbour cap"
@@ -203,13 +223,19 @@ def run_gb300(args):
     from sphgb.device import SceneBatch
     spec, state, desc = workload(args.workload)
     n = spec.n
+    log(f"workload {args.workload}: {n} particles")
     batch = SceneBatch([spec], device=str(dev))
     batch.load_states([state])
-    stream = torch.cuda.current_stream(dev)
-    # warm-up (also captures the one-step graph)
-    for _ in range(max(args.warmup, 0)):
-        batch.step(1, use_graph=True)
+    # every timed step is a full compute_next_state of the same resident
+    # input: the step writes to separate output buffers (see module docstring)
+    batch.bind_output(True)
     torch.cuda.synchronize()
+    log("state loaded")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 0)):
+        batch.step(1, use_graph=True)      # first call captures the one-step graph
+    torch.cuda.synchronize()
+    log(f"{args.warmup} warm-up steps done")
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -225,9 +251,11 @@ def run_gb300(args):
     ms = max_over_ranks(ms, world, dev)
     value = n * args.steps * world / (ms / 1e3)
     clocks = clk.summary()
+    log(f"timed {args.steps} steps: {ms:.3f} ms")
 
     # per-stage CUDA-event times (same kernels, no graph) -> dominant kernel roofline
     stages = batch.step_profiled(min(args.steps, 10))
+    log(f"stage ms: {stages}")
     dom = max(("density", "force_integrate", "rank_gather", "hash", "scatter"),
               key=lambda k: stages[k])
     peak, peak_kind = measured_peak_hbm()
@@ -243,26 +271,40 @@ def run_gb300(args):
                      "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
                      "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
 
-    # end to end through the C ABI host-buffer entry point, pinned host memory
+    # free-running simulation from the same start (informational): the
+    # reference's formulas make this scene blow up within a few steps
+    batch.bind_output(False)
+    k_free = min(args.steps, 10)
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    batch.step(k_free, use_graph=False)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    free = {"steps": k_free, "ms_per_step": f0.elapsed_time(f1) / k_free,
+            "nonfinite_particles": int((~torch.isfinite(batch.pos[:, :3]).all(dim=1)).sum())}
+    log(f"free running: {free}")
+
+    # end to end through the C ABI host-buffer entry point: each step copies
+    # the same FP64 AoS input from pinned host memory and the result back
     k_e2e = args.e2e_steps if args.e2e_steps is not None else min(args.steps, 10)
     pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa
-    h_pos = [pin((n, 3)), pin((n, 3))]
-    h_vel = [pin((n, 3)), pin((n, 3))]
-    h_rho = pin((n,))
-    h_pos[0][:] = state.position
-    h_vel[0][:] = state.velocity
-    batch.compute_next_state_host(h_pos[0], h_vel[0], h_pos[1], h_vel[1], h_rho)   # warm-up
+    h_pos, h_vel = pin((n, 3)), pin((n, 3))
+    o_pos, o_vel, o_rho = pin((n, 3)), pin((n, 3)), pin((n,))
+    h_pos[:] = state.position
+    h_vel[:] = state.velocity
+    batch.compute_next_state_host(h_pos, h_vel, o_pos, o_vel, o_rho)   # warm-up
     barrier(world)
     t0 = time.perf_counter()
     for i in range(k_e2e):
-        a, b = i % 2, (i + 1) % 2
-        batch.compute_next_state_host(h_pos[a], h_vel[a], h_pos[b], h_vel[b], h_rho)
+        batch.compute_next_state_host(h_pos, h_vel, o_pos, o_vel, o_rho)
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world, dev)
+    log(f"e2e {k_e2e} steps: {e2e_s:.3f} s")
     e2e = {"value": n * k_e2e * world / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 56 * n, "steps": k_e2e,
            "api": "sphgb_compute_next_state_host"}
-    assert np.isfinite(h_pos[k_e2e % 2]).all()
+    assert np.isfinite(o_rho).all()
 
     out = {"metric": "particle-steps/s (4M box, 1 GB300)" if args.workload == "config2"
            else "particle-steps/s (8k box)",
@@ -271,11 +313,14 @@ def run_gb300(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": desc, "particles": n, "voxels": batch.n_voxels,
                       "l2": "inputs larger than L2 (state + sort buffers ~0.4 GB > 129 MB)",
-                      "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step"},
+                      "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step",
+                      "input": "every step is a full step of the same resident step-0 state"},
            "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
+           "free_running": free,
            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(spec, state, args.cpu_steps)
+        log(f"cpu baseline: {out['cpu_baseline']}")
     if rank == 0:
         print(json.dumps(out), flush=True)
     batch.close()

@@ -77,6 +77,8 @@ struct SphgbCtx {
     int32_t* pidB = nullptr;
     double* pos64B = nullptr;
     float2* aux = nullptr;
+    int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
+    int32_t* big_count = nullptr;
     // bound (caller-owned) state
     float4* posA = nullptr;
     float4* velA = nullptr;
@@ -85,6 +87,11 @@ struct SphgbCtx {
     double* pos64A = nullptr;
     int32_t* scene_step = nullptr;
     bool bound = false;
+    // optional separate output of the step (the input state is then left untouched)
+    float4* out_pos = nullptr;
+    float4* out_vel = nullptr;
+    int32_t* out_pid = nullptr;
+    double* out_pos64 = nullptr;
     // state owned by the context for the host-buffer entry point when nothing is bound
     void* owned = nullptr;
     // staging for the host-buffer entry point
@@ -130,7 +137,8 @@ void free_ctx(SphgbCtx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
-                    c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials};
+                    c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials,
+                    c->big_list, c->big_count};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -397,51 +405,51 @@ inline int blocks(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-// enqueue one full step on stream st
-int enqueue_step(SphgbCtx* c, cudaStream_t st) {
-    const Launch L = c->launch(st);
-    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(c->vcount, 0, sizeof(int32_t) * c->v_total, st));
-    SPHGB_CUDA(launch_hash_count(L, c->posA, c->cell, c->slot, c->vcount));
-    SPHGB_CUDA(launch_scan(L, c->vcount, c->vstart, c->tile_sums, c->n_tiles));
-    SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, c->pidA, c->vstart, c->tmp_pid));
-    SPHGB_CUDA(launch_rank_gather(L, c->cell, c->pidA, c->tmp_pid, c->vstart, c->vcount, c->posA,
-                                  c->velA, c->any_pipe ? c->pos64A : nullptr, c->posB, c->velB,
-                                  c->pidB, c->any_pipe ? c->pos64B : nullptr));
-    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux));
-    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB,
-                                c->any_pipe ? c->pos64B : nullptr, c->vstart, c->vcount,
-                                c->scene_step, c->posA, c->velA, c->pidA,
-                                c->any_pipe ? c->pos64A : nullptr, nullptr));
-    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
-    SPHGB_CUDA(cudaGetLastError());
+// hash + scan + scatter + big-voxel sort + rank-gather: state (any order) ->
+// voxel-sorted copy and voxel table
+int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const float4* vel,
+                     const int32_t* pid, const double* pos64, float4* pos_o, float4* vel_o,
+                     int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
+                     cudaEvent_t* ev = nullptr) {
+    cudaStream_t st = L.stream;
+    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * c->v_total, st));
+    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, sizeof(int32_t), st));
+    SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
+    SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, c->n_tiles));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[1], st));
+    SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, pid, vstart, vcount, c->tmp_pid, c->big_list,
+                              c->big_count));
+    SPHGB_CUDA(launch_sort_big(L, c->big_list, c->big_count, vstart, vcount, c->tmp_pid));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[2], st));
+    SPHGB_CUDA(launch_rank_gather(L, c->cell, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
+                                  pos_o, vel_o, pid_o, pos64_o));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[3], st));
     return SPHGB_OK;
 }
 
-// one step with an event after every stage: ev[0] before, ev[i+1] after stage i
-int enqueue_step_profiled(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev) {
+// enqueue one full step on stream st; ev (optional, 8 events): ev[0] at the
+// start and ev[k] after stage k (see SPHGB_PROFILE_STAGES)
+int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     const Launch L = c->launch(st);
-    SPHGB_CUDA(cudaEventRecord(ev[0], st));
-    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(c->vcount, 0, sizeof(int32_t) * c->v_total, st));
-    SPHGB_CUDA(launch_hash_count(L, c->posA, c->cell, c->slot, c->vcount));
-    SPHGB_CUDA(cudaEventRecord(ev[1], st));
-    SPHGB_CUDA(launch_scan(L, c->vcount, c->vstart, c->tile_sums, c->n_tiles));
-    SPHGB_CUDA(cudaEventRecord(ev[2], st));
-    SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, c->pidA, c->vstart, c->tmp_pid));
-    SPHGB_CUDA(cudaEventRecord(ev[3], st));
-    SPHGB_CUDA(launch_rank_gather(L, c->cell, c->pidA, c->tmp_pid, c->vstart, c->vcount, c->posA,
-                                  c->velA, c->any_pipe ? c->pos64A : nullptr, c->posB, c->velB,
-                                  c->pidB, c->any_pipe ? c->pos64B : nullptr));
-    SPHGB_CUDA(cudaEventRecord(ev[4], st));
+    double* p64A = c->any_pipe ? c->pos64A : nullptr;
+    double* p64B = c->any_pipe ? c->pos64B : nullptr;
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
+    int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
+                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr);
+    if (rc) return rc;
     SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux));
-    SPHGB_CUDA(cudaEventRecord(ev[5], st));
-    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB,
-                                c->any_pipe ? c->pos64B : nullptr, c->vstart, c->vcount,
-                                c->scene_step, c->posA, c->velA, c->pidA,
-                                c->any_pipe ? c->pos64A : nullptr, nullptr));
-    SPHGB_CUDA(cudaEventRecord(ev[6], st));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
+    const bool sep = c->out_pos != nullptr;
+    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB, p64B, c->vstart,
+                                c->vcount, c->scene_step, sep ? c->out_pos : c->posA,
+                                sep ? c->out_vel : c->velA, sep ? c->out_pid : c->pidA,
+                                c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr,
+                                nullptr));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[6], st));
     k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
     SPHGB_CUDA(cudaGetLastError());
-    SPHGB_CUDA(cudaEventRecord(ev[7], st));
+    if (ev) SPHGB_CUDA(cudaEventRecord(ev[7], st));
     return SPHGB_OK;
 }
 
@@ -481,7 +489,7 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
         d.v_begin = (int32_t)v_tot;
         c->h_pbegin[i] = (int32_t)n_tot;
         n_tot += scenes[i].particle_count;
-        v_tot += d.v_count;
+        v_tot += d.v_count + 1;   // + the scene's overflow bucket
         if (n_tot > (int64_t)0x7fffffff - 1 || v_tot > (int64_t)0x7fffffff - 1) {
             free_ctx(c);
             return fail(SPHGB_ERR_RANGE, "particles or voxels over 2^31 in one context");
@@ -516,6 +524,8 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
     rc = rc ? rc : dalloc(&c->velB, N);
     rc = rc ? rc : dalloc(&c->pidB, N);
     rc = rc ? rc : dalloc(&c->aux, N);
+    rc = rc ? rc : dalloc(&c->big_list, N / kBigVoxel + 1);
+    rc = rc ? rc : dalloc(&c->big_count, 1);
     if (c->any_pipe) rc = rc ? rc : dalloc(&c->pos64B, 3 * N);
     rc = rc ? rc : dalloc(&c->d_chunks, chunks.size());
     rc = rc ? rc : dalloc(&c->d_partials, chunks.size() * 6);
@@ -581,6 +591,24 @@ int sphgb_ctx_bind_state(SphgbCtx* ctx, float* d_pos, float* d_vel, float* d_rho
     return SPHGB_OK;
 }
 
+int sphgb_ctx_bind_output(SphgbCtx* ctx, float* d_pos_out, float* d_vel_out, int32_t* d_pid_out,
+                          double* d_pos64_out) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    const bool any = d_pos_out || d_vel_out || d_pid_out || d_pos64_out;
+    if (any && ctx->n > 0 && (!d_pos_out || !d_vel_out || !d_pid_out ||
+                              (ctx->any_pipe && !d_pos64_out)))
+        return fail(SPHGB_ERR_INVALID, "bind all output buffers or none");
+    if (((uintptr_t)d_pos_out | (uintptr_t)d_vel_out) & 15u)
+        return fail(SPHGB_ERR_INVALID, "position/velocity buffers must be 16-byte aligned");
+    ctx->out_pos = reinterpret_cast<float4*>(d_pos_out);
+    ctx->out_vel = reinterpret_cast<float4*>(d_vel_out);
+    ctx->out_pid = d_pid_out;
+    ctx->out_pos64 = d_pos64_out;
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    return SPHGB_OK;
+}
+
 int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double* d_vel_aos,
                            void* stream) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
@@ -601,10 +629,12 @@ int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
     if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
     if (ctx->n == 0) return SPHGB_OK;
     cudaStream_t st = as_stream(stream);
-    k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes,
-                                                  ctx->n, ctx->posA, ctx->velA, ctx->rho,
-                                                  ctx->pidA, ctx->pos64A, d_pos_aos, d_vel_aos,
-                                                  d_rho);
+    // the latest step's result: the output buffers when bound, else the state
+    const bool sep = ctx->out_pos != nullptr;
+    k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(
+        ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sep ? ctx->out_pos : ctx->posA,
+        sep ? ctx->out_vel : ctx->velA, ctx->rho, sep ? ctx->out_pid : ctx->pidA,
+        sep ? ctx->out_pos64 : ctx->pos64A, d_pos_aos, d_vel_aos, d_rho);
     SPHGB_CUDA(cudaGetLastError());
     return SPHGB_OK;
 }
@@ -657,7 +687,7 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
         cudaError_t err = cudaEventCreate(&e);
         if (err != cudaSuccess) { rc = cuda_fail(err, "cudaEventCreate"); break; }
     }
-    for (int i = 0; i < n_steps && rc == SPHGB_OK; ++i) rc = enqueue_step_profiled(ctx, st, &ev[(size_t)i * 8]);
+    for (int i = 0; i < n_steps && rc == SPHGB_OK; ++i) rc = enqueue_step(ctx, st, &ev[(size_t)i * 8]);
     if (rc == SPHGB_OK) {
         cudaError_t err = cudaStreamSynchronize(st);
         if (err != cudaSuccess) rc = cuda_fail(err, "cudaStreamSynchronize");
@@ -749,14 +779,11 @@ int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_unca
     if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
     cudaStream_t st = as_stream(stream);
     const Launch L = ctx->launch(st);
-    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * ctx->v_total, st));
-    SPHGB_CUDA(launch_hash_count(L, ctx->posA, ctx->cell, ctx->slot, ctx->vcount));
-    SPHGB_CUDA(launch_scan(L, ctx->vcount, ctx->vstart, ctx->tile_sums, ctx->n_tiles));
-    SPHGB_CUDA(launch_scatter(L, ctx->cell, ctx->slot, ctx->pidA, ctx->vstart, ctx->tmp_pid));
-    SPHGB_CUDA(launch_rank_gather(L, ctx->cell, ctx->pidA, ctx->tmp_pid, ctx->vstart, ctx->vcount,
-                                  ctx->posA, ctx->velA, ctx->any_pipe ? ctx->pos64A : nullptr,
-                                  ctx->posB, ctx->velB, ctx->pidB,
-                                  ctx->any_pipe ? ctx->pos64B : nullptr));
+    int rc = enqueue_organize(ctx, L, ctx->posA, ctx->velA, ctx->pidA,
+                              ctx->any_pipe ? ctx->pos64A : nullptr, ctx->posB, ctx->velB,
+                              ctx->pidB, ctx->any_pipe ? ctx->pos64B : nullptr, ctx->vstart,
+                              ctx->vcount);
+    if (rc) return rc;
     // per sorted slot into the scratch id buffers, then to original order
     SPHGB_CUDA(launch_neighbours(L, ctx->posB, ctx->vstart, ctx->vcount, nullptr, 0, ctx->cell,
                                  ctx->slot));
@@ -789,17 +816,11 @@ int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
         return fail(SPHGB_ERR_INVALID, "pass both FP64 position buffers or neither");
     cudaStream_t st = as_stream(stream);
     const Launch L = ctx->launch(st);
-    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(d_voxel_count, 0, sizeof(int32_t) * ctx->v_total, st));
-    SPHGB_CUDA(launch_hash_count(L, reinterpret_cast<const float4*>(d_pos), ctx->cell, ctx->slot,
-                                 d_voxel_count));
-    SPHGB_CUDA(launch_scan(L, d_voxel_count, d_voxel_start, ctx->tile_sums, ctx->n_tiles));
-    SPHGB_CUDA(launch_scatter(L, ctx->cell, ctx->slot, d_pid, d_voxel_start, ctx->tmp_pid));
-    SPHGB_CUDA(launch_rank_gather(L, ctx->cell, d_pid, ctx->tmp_pid, d_voxel_start, d_voxel_count,
-                                  reinterpret_cast<const float4*>(d_pos),
-                                  reinterpret_cast<const float4*>(d_vel), d_pos64,
-                                  reinterpret_cast<float4*>(d_pos_out),
-                                  reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out));
-    return SPHGB_OK;
+    return enqueue_organize(ctx, L, reinterpret_cast<const float4*>(d_pos),
+                            reinterpret_cast<const float4*>(d_vel), d_pid, d_pos64,
+                            reinterpret_cast<float4*>(d_pos_out),
+                            reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out,
+                            d_voxel_start, d_voxel_count);
 }
 
 int sphgb_neighbours(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_voxel_start,

@@ -13,6 +13,10 @@
 //      into that slot.  The result is the reference's (voxel, particle id)
 //      order exactly, independent of atomic arrival order and of the input
 //      order of the state.
+// Voxels with more than kBigVoxel members (dense clusters, the overflow bucket
+// of non-finite particles) have their member ids sorted by one block each
+// between 3 and 4, and the rank is a binary search, so the pass stays
+// O(n log n) however the particles cluster.
 #include "sphgb_internal.cuh"
 
 namespace sphgb {
@@ -62,10 +66,15 @@ k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
     const float4 p = __ldg(pos + s);
-    const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
-    const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
-    const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
-    const int vid = sc.v_begin + vx + vy * sc.dims[0] + vz * sc.dims[0] * sc.dims[1];
+    int vid;
+    if (finite3(p)) {
+        const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
+        const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
+        const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
+        vid = sc.v_begin + vx + vy * sc.dims[0] + vz * sc.dims[0] * sc.dims[1];
+    } else {
+        vid = sc.v_begin + sc.v_count;   // overflow bucket
+    }
     cell[s] = vid;
     slot[s] = atomicAdd(vcount + vid, 1);
 }
@@ -154,10 +163,68 @@ k_tile_scan(const int32_t* __restrict__ vcount, int v_total, const int32_t* __re
 __global__ void __launch_bounds__(kBlock)
 k_scatter(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ slot,
           const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
-          int32_t* __restrict__ tmp_pid) {
+          const int32_t* __restrict__ vcount, int32_t* __restrict__ tmp_pid,
+          int32_t* __restrict__ big_list, int32_t* __restrict__ big_count) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    tmp_pid[__ldg(vstart + cell[s]) + slot[s]] = pid[s];
+    const int vid = cell[s];
+    const int sl = slot[s];
+    tmp_pid[__ldg(vstart + vid) + sl] = pid[s];
+    if (sl == 0 && __ldg(vcount + vid) > kBigVoxel) big_list[atomicAdd(big_count, 1)] = vid;
+}
+
+// One block per big voxel (grid-stride over the list): sorts the voxel's
+// member ids ascending with a bitonic network whose comparators all put the
+// smaller value at the lower index, so the segment is padded to a power of
+// two implicitly (comparators reaching past the end are no-ops).  Segments up
+// to kSmemSort ids are sorted in shared memory, longer ones in place in global
+// memory.
+constexpr int kSortThreads = 1024;
+constexpr int kSmemSort = 8192;
+
+__device__ __forceinline__ void bitonic_pass(int32_t* a, int c, int n2, int k, int j) {
+    const int half = n2 >> 1;
+    for (int t = threadIdx.x; t < half; t += kSortThreads) {
+        int i, p;
+        if (j == (k >> 1)) {            // first step of a merge: mirror within the k-block
+            i = (t / j) * k + (t % j);
+            p = i ^ (k - 1);
+        } else {                        // half-cleaner
+            i = (t / j) * 2 * j + (t % j);
+            p = i + j;
+        }
+        if (p < c) {
+            const int32_t x = a[i], y = a[p];
+            if (y < x) { a[i] = y; a[p] = x; }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+k_sort_big(const int32_t* __restrict__ big_list, const int32_t* __restrict__ big_count,
+           const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+           int32_t* __restrict__ tmp_pid) {
+    __shared__ int32_t sm[kSmemSort];
+    const int nb = *big_count;
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const int vid = big_list[b];
+        const int st = vstart[vid], c = vcount[vid];
+        int n2 = 1;
+        while (n2 < c) n2 <<= 1;
+        const bool in_smem = n2 <= kSmemSort;
+        int32_t* a = in_smem ? sm : tmp_pid + st;
+        if (in_smem)
+            for (int i = threadIdx.x; i < c; i += kSortThreads) sm[i] = tmp_pid[st + i];
+        __syncthreads();
+        for (int k = 2; k <= n2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                bitonic_pass(a, c, n2, k, j);
+                __syncthreads();
+            }
+        if (in_smem)
+            for (int i = threadIdx.x; i < c; i += kSortThreads) tmp_pid[st + i] = sm[i];
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -174,7 +241,16 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
     const int st = __ldg(vstart + vid);
     const int c = __ldg(vcount + vid);
     int r = 0;
-    for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
+    if (c <= kBigVoxel) {
+        for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
+    } else {                            // sorted by k_sort_big: lower bound of p
+        int lo = 0, hi = c;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(tmp_pid + st + mid) < p) lo = mid + 1; else hi = mid;
+        }
+        r = lo;
+    }
     const int d = st + r;
     pid_out[d] = p;
     pos_out[d] = __ldg(pos + s);
@@ -210,9 +286,19 @@ cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
 }
 
 cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* slot,
-                           const int32_t* pid, const int32_t* vstart, int32_t* tmp_pid) {
+                           const int32_t* pid, const int32_t* vstart, const int32_t* vcount,
+                           int32_t* tmp_pid, int32_t* big_list, int32_t* big_count) {
     if (L.n == 0) return cudaSuccess;
-    k_scatter<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, slot, pid, vstart, tmp_pid);
+    k_scatter<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, slot, pid, vstart, vcount,
+                                                         tmp_pid, big_list, big_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
+                            const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid) {
+    if (L.n == 0) return cudaSuccess;
+    // one block per SM: enough for the rare big voxels, idle blocks exit at once
+    k_sort_big<<<152, kSortThreads, 0, L.stream>>>(big_list, big_count, vstart, vcount, tmp_pid);
     return cudaGetLastError();
 }
 

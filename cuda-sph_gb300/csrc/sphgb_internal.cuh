@@ -26,13 +26,15 @@ constexpr int kBlock = 256;
 // One scene as the kernels see it (built on the host from SphgbSceneParams).
 struct SceneDev {
     int32_t p_begin, p_count;   // slots [p_begin, p_begin + p_count) in sorted state
-    int32_t v_begin, v_count;   // voxel table range
+    int32_t v_begin, v_count;   // voxel table range: v_count voxels of the grid plus one
+                                // overflow bucket (index v_begin + v_count) that holds
+                                // particles with non-finite positions and is never walked
     int32_t dims[3];            // table dims, ceil(space / voxel)
     int32_t wdims[3];           // walk dims (== dims, or truncated)
     float vs[3];                // voxel size
     float h, h2, h2_lo, h2_hi;  // INF_R, INF_R^2 and the FP32 guard band
     float cull2;                // squared distance beyond which a voxel is skipped
-    float w_const, grad_w_const, lap_w_const;
+    float w_const, grad_w_const, lap_w_const;  // W_CONST h^6, GRAD_W_CONST h^2, LAP_W_CONST h
     float mass, rho0, k, visc, damp, dt;
     float ext[3];
     float space[3];
@@ -82,17 +84,21 @@ static __device__ __noinline__ bool within_exact(float xi, float yi, float zi, f
 }
 
 // d2 of the pair in FP32; returns the reference's decision.
-__device__ __forceinline__ bool within(const float4& pi, const float4& pj, const SceneDev& sc,
-                                       float& dx, float& dy, float& dz, float& d2) {
+__device__ __forceinline__ bool within(const float4& pi, const float4& pj, float h2_lo, float h2_hi,
+                                       double h_d, float& dx, float& dy, float& dz, float& d2) {
     dx = __fsub_rn(pi.x, pj.x);
     dy = __fsub_rn(pi.y, pj.y);
     dz = __fsub_rn(pi.z, pj.z);
     d2 = __fmul_rn(dx, dx);
     d2 = __fmaf_rn(dy, dy, d2);
     d2 = __fmaf_rn(dz, dz, d2);
-    if (d2 < sc.h2_lo) return true;
-    if (d2 > sc.h2_hi) return false;
-    return within_exact(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, sc.h_d);
+    if (d2 < h2_lo) return true;
+    if (d2 > h2_hi) return false;
+    return within_exact(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z, h_d);
+}
+
+__device__ __forceinline__ bool finite3(const float4& p) {
+    return isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
 }
 
 // ---- Kahan summation ------------------------------------------------------
@@ -107,46 +113,71 @@ struct Kahan {
 };
 
 // ---- the 27-voxel walk ----------------------------------------------------
+// Scene geometry the walk needs, loaded once per thread into registers.
+struct WalkGeom {
+    float vs0, vs1, vs2;
+    int d0, d1, d2;        // table dims
+    int w0, w1, w2;        // walk dims
+    int v_begin;
+    float h2_lo, h2_hi, cull2;
+    double h_d;
+    int cap;
+    bool cull;
+};
+
+__device__ __forceinline__ WalkGeom load_geom(const SceneDev& sc) {
+    WalkGeom g;
+    g.vs0 = sc.vs[0]; g.vs1 = sc.vs[1]; g.vs2 = sc.vs[2];
+    g.d0 = sc.dims[0]; g.d1 = sc.dims[1]; g.d2 = sc.dims[2];
+    g.w0 = sc.wdims[0]; g.w1 = sc.wdims[1]; g.w2 = sc.wdims[2];
+    g.v_begin = sc.v_begin;
+    g.h2_lo = sc.h2_lo; g.h2_hi = sc.h2_hi; g.cull2 = sc.cull2;
+    g.h_d = sc.h_d;
+    g.cap = sc.cap;
+    g.cull = !sc.walk_trunc;
+    return g;
+}
+
 // Visits neighbours of a particle in the reference's order (voxel_kernels.py:
 // 46-61 dx outer, dy, dz inner; members in ascending particle id, which is
 // slot order inside a voxel) and stops after `cap` accepted neighbours
 // (self included, :77-84).  visit(j, dx, dy, dz, d2) is called per accepted
-// neighbour slot j.  Returns the number accepted.
+// neighbour slot j.  Returns the number accepted.  A particle with a
+// non-finite coordinate has no neighbours (every distance test fails).
 template <class Visit>
-__device__ __forceinline__ int walk(const float4 pi, const SceneDev& sc,
+__device__ __forceinline__ int walk(const float4 pi, const WalkGeom& g,
                                     const int32_t* __restrict__ vstart,
                                     const int32_t* __restrict__ vcount,
                                     const float4* __restrict__ pos, int cap, Visit&& visit) {
-    const int cx = voxel_coord(pi.x, sc.vs[0], sc.dims[0]);
-    const int cy = voxel_coord(pi.y, sc.vs[1], sc.dims[1]);
-    const int cz = voxel_coord(pi.z, sc.vs[2], sc.dims[2]);
-    const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
+    if (!finite3(pi)) return 0;
+    const int cx = voxel_coord(pi.x, g.vs0, g.d0);
+    const int cy = voxel_coord(pi.y, g.vs1, g.d1);
+    const int cz = voxel_coord(pi.z, g.vs2, g.d2);
     // squared distances to the lower/upper faces of the own voxel, used to skip
     // voxels that lie entirely beyond h (only when walk dims == table dims)
-    const float fx = pi.x - (float)cx * sc.vs[0];
-    const float fy = pi.y - (float)cy * sc.vs[1];
-    const float fz = pi.z - (float)cz * sc.vs[2];
-    const float gx0 = fx * fx, gx2 = (sc.vs[0] - fx) * (sc.vs[0] - fx);
-    const float gy0 = fy * fy, gy2 = (sc.vs[1] - fy) * (sc.vs[1] - fy);
-    const float gz0 = fz * fz, gz2 = (sc.vs[2] - fz) * (sc.vs[2] - fz);
-    const bool cull = !sc.walk_trunc;
+    const float fx = pi.x - (float)cx * g.vs0;
+    const float fy = pi.y - (float)cy * g.vs1;
+    const float fz = pi.z - (float)cz * g.vs2;
+    const float gx0 = fx * fx, gx2 = (g.vs0 - fx) * (g.vs0 - fx);
+    const float gy0 = fy * fy, gy2 = (g.vs1 - fy) * (g.vs1 - fy);
+    const float gz0 = fz * fz, gz2 = (g.vs2 - fz) * (g.vs2 - fz);
     int n = 0;
 #pragma unroll 1
     for (int ddx = 0; ddx < 3; ++ddx) {
         const int nx = cx + ddx - 1;
-        if (nx < 0 || nx >= w0) continue;
+        if (nx < 0 || nx >= g.w0) continue;
         const float gx = ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f);
 #pragma unroll 1
         for (int ddy = 0; ddy < 3; ++ddy) {
             const int ny = cy + ddy - 1;
-            if (ny < 0 || ny >= w1) continue;
+            if (ny < 0 || ny >= g.w1) continue;
             const float gxy = gx + (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
 #pragma unroll 1
             for (int ddz = 0; ddz < 3; ++ddz) {
                 const int nz = cz + ddz - 1;
-                if (nz < 0 || nz >= w2) continue;
-                if (cull && gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > sc.cull2) continue;
-                const int vid = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
+                if (nz < 0 || nz >= g.w2) continue;
+                if (g.cull && gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > g.cull2) continue;
+                const int vid = g.v_begin + nx + ny * g.w0 + nz * g.w0 * g.w1;
                 const int c = __ldg(vcount + vid);
                 if (c == 0) continue;
                 const int s0 = __ldg(vstart + vid);
@@ -155,7 +186,7 @@ __device__ __forceinline__ int walk(const float4 pi, const SceneDev& sc,
                     const int j = s0 + m;
                     const float4 pj = __ldg(pos + j);
                     float dx, dy, dz, d2;
-                    if (within(pi, pj, sc, dx, dy, dz, d2)) {
+                    if (within(pi, pj, g.h2_lo, g.h2_hi, g.h_d, dx, dy, dz, d2)) {
                         visit(j, dx, dy, dz, d2);
                         if (++n >= cap) return n;
                     }
@@ -336,7 +367,13 @@ cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
                         int32_t* tile_sums, int n_tiles);
 int scan_tiles(int v_total);
 cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* slot,
-                           const int32_t* pid, const int32_t* vstart, int32_t* tmp_pid);
+                           const int32_t* pid, const int32_t* vstart, const int32_t* vcount,
+                           int32_t* tmp_pid, int32_t* big_list, int32_t* big_count);
+// voxels with more than kBigVoxel members get their member ids sorted by one
+// block each (the rank-gather then binary-searches them instead of counting)
+constexpr int kBigVoxel = 64;
+cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
+                            const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
 cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
                                const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,

@@ -25,10 +25,11 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const WalkGeom g = load_geom(sc);
     const float4 pi = __ldg(pos + s);
     const float inv_h2 = 1.0f / sc.h2;
     Kahan acc;
-    walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float, float, float, float d2) {
+    walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
         if (j != s) {
             const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
             acc.add(u * u * u);
@@ -55,6 +56,7 @@ k_aux(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, i
 
 struct ForceSums {
     Kahan px, py, pz, vx, vy, vz;
+    int terms = 0;   // neighbours other than self
 };
 
 // pressure_kernel (voxel_kernels.py:136-171) and viscosity_kernel (:175-211)
@@ -65,25 +67,27 @@ struct ForceSums {
 //         lap W = LAP_W_CONST (h - r)                        (base_kernels.py:24-27)
 // with (h - r) written as h (1 - r/h).
 __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4& vi,
-                                           float a_i, const SceneDev& sc,
+                                           float a_i, const SceneDev& sc, const WalkGeom& geom,
                                            const float4* __restrict__ pos,
                                            const float4* __restrict__ vel,
                                            const float2* __restrict__ aux,
                                            const int32_t* __restrict__ vstart,
                                            const int32_t* __restrict__ vcount, ForceSums& f) {
     const float inv_h = 1.0f / sc.h;
-    walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float dx, float dy, float dz, float d2) {
+    const float gw = sc.grad_w_const, lw = sc.lap_w_const;
+    walk(pi, geom, vstart, vcount, pos, geom.cap, [&](int j, float dx, float dy, float dz, float d2) {
         if (j == s) return;
+        ++f.terms;
         const float2 aj = __ldg(aux + j);
         const float4 vj = __ldg(vel + j);
         const float r = sqrtf(d2);
         const float inv_r = 1.0f / r;
         const float t = __fmaf_rn(-r, inv_h, 1.0f);
-        const float g = ((a_i + aj.x) * sc.grad_w_const) * (t * t) * inv_r;
+        const float g = ((a_i + aj.x) * gw) * (t * t) * inv_r;
         f.px.add(g * dx);
         f.py.add(g * dy);
         f.pz.add(g * dz);
-        const float l = (sc.lap_w_const * t) * aj.y;
+        const float l = (lw * t) * aj.y;
         f.vx.add(l * (vj.x - vi.x));
         f.vy.add(l * (vj.y - vi.y));
         f.vz.add(l * (vj.z - vi.z));
@@ -91,6 +95,13 @@ __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4
 }
 
 __device__ __forceinline__ float clamp1(float x) { return x < 1.0f ? x : 1.0f; }  // min(1, x)
+
+// viscosity term of one component: the reference multiplies every neighbour
+// term by MASS * VISC / rho_i (voxel_kernels.py:207-208), so with no
+// neighbour terms the sum is 0 even when rho_i is 0
+__device__ __forceinline__ float visc_term(const ForceSums& f, float sum, float vscale) {
+    return clamp1(f.terms ? sum * vscale : 0.0f);
+}
 
 __global__ void __launch_bounds__(kBlock)
 k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
@@ -105,11 +116,11 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
     const float4 vi = __ldg(vel + s);
     const float2 ai = __ldg(aux + s);
     ForceSums f;
-    force_sums(s, pi, vi, ai.x, sc, pos, vel, aux, vstart, vcount, f);
+    force_sums(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
     const float vscale = sc.mass * sc.visc * ai.y;
     pressure[s] = make_float4(f.px.s, f.py.s, f.pz.s, 0.0f);
-    viscosity[s] = make_float4(clamp1(f.vx.s * vscale), clamp1(f.vy.s * vscale),
-                               clamp1(f.vz.s * vscale), 0.0f);
+    viscosity[s] = make_float4(visc_term(f, f.vx.s, vscale), visc_term(f, f.vy.s, vscale),
+                               visc_term(f, f.vz.s, vscale), 0.0f);
 }
 
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
@@ -134,13 +145,13 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const float2 ai = __ldg(aux + s);
     const float rho_i = __ldg(rho + s);
     ForceSums f;
-    force_sums(s, pi, vi, ai.x, sc, pos, vel, aux, vstart, vcount, f);
+    force_sums(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
     const float vscale = sc.mass * sc.visc * ai.y;
     // result_force = ext + -P + V (base_kernels.py:46-52)
     float F[3];
-    F[0] = (sc.ext[0] + -f.px.s) + clamp1(f.vx.s * vscale);
-    F[1] = (sc.ext[1] + -f.py.s) + clamp1(f.vy.s * vscale);
-    F[2] = (sc.ext[2] + -f.pz.s) + clamp1(f.vz.s * vscale);
+    F[0] = (sc.ext[0] + -f.px.s) + visc_term(f, f.vx.s, vscale);
+    F[1] = (sc.ext[1] + -f.py.s) + visc_term(f, f.vy.s, vscale);
+    F[2] = (sc.ext[2] + -f.pz.s) + visc_term(f, f.vz.s, vscale);
     float v[3] = {vi.x, vi.y, vi.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
@@ -191,18 +202,18 @@ k_neighbours(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
              int32_t* __restrict__ n_uncapped) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const WalkGeom g = load_geom(scenes[scene_of(s, pbegin, n_scenes)]);
     const float4 pi = __ldg(pos + s);
     int k = 0;
     int32_t* li = list ? list + (size_t)s * stride : nullptr;
-    const int c = walk(pi, sc, vstart, vcount, pos, sc.cap, [&](int j, float, float, float, float) {
+    const int c = walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
         if (li && k < stride) li[k] = j;
         ++k;
     });
     if (li) for (int t = c; t < stride; ++t) li[t] = -1;
     if (n_capped) n_capped[s] = c;
     if (n_uncapped)
-        n_uncapped[s] = walk(pi, sc, vstart, vcount, pos, 0x7fffffff,
+        n_uncapped[s] = walk(pi, g, vstart, vcount, pos, 0x7fffffff,
                              [&](int, float, float, float, float) {});
 }
 

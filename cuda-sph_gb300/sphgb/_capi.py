@@ -64,6 +64,7 @@ SIGNATURES = [
     ("sphgb_ctx_destroy", _I, [_VP]),
     ("sphgb_ctx_sizes", _I, [_VP, C.POINTER(_I64), C.POINTER(_I64)]),
     ("sphgb_ctx_bind_state", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    ("sphgb_ctx_bind_output", _I, [_VP, _VP, _VP, _VP, _VP]),
     ("sphgb_ctx_load_aos_f64", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_ctx_store_aos_f64", _I, [_VP, _VP, _VP, _VP, _VP]),
     ("sphgb_ctx_step", _I, [_VP, _I, _I, _VP]),
@@ -76,7 +77,7 @@ SIGNATURES = [
     ("sphgb_neighbours", _I, [_VP, _VP, _VP, _VP, _VP, _I, _VP, _VP, _VP]),
     ("sphgb_density", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     ("sphgb_forces", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
-    ("sphgb_integrate", _I, [_VP] + [_VP] * 14 + [_VP]),
+    ("sphgb_integrate", _I, [_VP] + [_VP] * 13 + [_VP]),
     ("sphgb_pipe_find_segment", _I, [_VP, _I, _VP, _I, _VP, _VP]),
     ("sphgb_pipe_is_out", _I, [_VP, _VP, _I, _VP, _I, _VP, _VP, _VP]),
     ("sphgb_pipe_x_at_segment_beginning", _I, [_VP, _I, _VP, _I, _VP, _VP]),

@@ -131,6 +131,25 @@ class SceneBatch:
         except Exception:
             pass
 
+    def bind_output(self, enable: bool = True) -> None:
+        """With enable, every step writes its result to separate output
+        tensors (self.out_pos, self.out_vel, self.out_pid, self.out_pos64) and
+        leaves the bound state unchanged, so repeated steps all start from it."""
+        torch = self._torch
+        if enable:
+            dev, n = self.device, max(self.n, 1)
+            self.out_pos = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+            self.out_vel = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+            self.out_pid = torch.zeros((n,), dtype=torch.int32, device=dev)
+            self.out_pos64 = torch.zeros((n if self.any_pipe else 1, 3), dtype=torch.float64,
+                                         device=dev)
+            _capi.call("sphgb_ctx_bind_output", self._ctx, self.out_pos.data_ptr(),
+                       self.out_vel.data_ptr(), self.out_pid.data_ptr(),
+                       self.out_pos64.data_ptr() if self.any_pipe else None)
+        else:
+            _capi.call("sphgb_ctx_bind_output", self._ctx, None, None, None, None)
+            self.out_pos = self.out_vel = self.out_pid = self.out_pos64 = None
+
     # -- state in / out --------------------------------------------------
     def load_states(self, states: Sequence[SimulationState], stream=None) -> None:
         """Upload host states (SimulationState per scene, original particle order)."""

@@ -99,7 +99,9 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes,
                      const double* pipe_rows_table, int n_pipe_rows_total,
                      SphgbCtx** out_ctx);
 int sphgb_ctx_destroy(SphgbCtx* ctx);
-/* Total particles / voxels over all scenes of the context. */
+/* Total particles / voxel-table entries over all scenes of the context.  A
+ * scene's table has ceil(space/voxel) voxels plus one overflow entry (last)
+ * that collects particles with non-finite coordinates; no walk visits it. */
 int sphgb_ctx_sizes(const SphgbCtx* ctx, int64_t* n_particles, int64_t* n_voxels);
 
 /* Bind caller-owned device state (voxel-sorted order, see conventions).
@@ -109,12 +111,21 @@ int sphgb_ctx_sizes(const SphgbCtx* ctx, int64_t* n_particles, int64_t* n_voxels
 int sphgb_ctx_bind_state(SphgbCtx* ctx, float* d_pos, float* d_vel, float* d_rho,
                          int32_t* d_pid, double* d_pos64, int32_t* d_scene_step);
 
+/* Optional: write the next state of every step to separate buffers instead
+ * of back into the bound state, which is then left unchanged (repeated steps
+ * all start from it).  Pass four NULLs to return to in-place stepping.
+ * d_pos64_out is required when any scene is in pipe mode. */
+int sphgb_ctx_bind_output(SphgbCtx* ctx, float* d_pos_out, float* d_vel_out, int32_t* d_pid_out,
+                          double* d_pos64_out);
+
 /* Load state from FP64 AoS arrays in original particle order (the layout of
  * SimulationState.position / .velocity, common/data_classes.py:81-85) already
  * on the device; sets pid = identity and the FP64 accumulator. */
 int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double* d_vel_aos,
                            void* stream);
-/* Write the bound state back as FP64 AoS in original particle order. */
+/* Write the latest state (the output buffers when bound with
+ * sphgb_ctx_bind_output, else the bound state) as FP64 AoS in original
+ * particle order; d_rho receives the density of the latest step. */
 int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
                             double* d_rho, void* stream);
 

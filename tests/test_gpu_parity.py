@@ -3,11 +3,15 @@ vectors recorded from the reference's own step code and (b) the FP64 oracle.
 
 Bit-exact: voxel ids, sorted (voxel, particle id) order, voxel table, ordered
 capped neighbour lists, capped and uncapped neighbour counts.
-FP32 tolerances (stated per quantity below, relative to the FP64 result):
+FP32 tolerances, relative to the FP64 result of the same inputs:
   density                      1e-5 of |rho|
-  pressure / viscosity terms   2e-4 of the sum of |term_j| over neighbours
-  next velocity                2e-4 of |v| + |F / rho * dt|
-  next position                1e-6 of max(|x|, 1)
+  pressure / viscosity terms   2e-4 of S, the sum of |term_j| over neighbours
+                               (the terms cancel, so |P| itself can be << S)
+  next velocity   |dv| <= 2e-4 (S_P + S_V + |ext|) / rho * dt + 2^-20 |v|
+  next position   |dx| <= (velocity bound) * dt + 2^-20 max(|x|, h)
+Pipe particles whose wall response fired (the collision geometry divides by
+sin(angle) + 0.001, util_kernels.py:119-121) are held to 1e-3 of
+max(|x|, h) and of |v| + the velocity bound.
 """
 import numpy as np
 import pytest
@@ -33,7 +37,7 @@ def _cases():
     return out
 
 
-def check_step(g, exp, ok, scales, dt, label):
+def check_step(g, exp, ok, scales, dt, label, ext=(0.0, 0.0, 0.0), h=1.0, collided=None):
     """Compare GPU stage outputs g with expected exp (dict of arrays) on mask ok."""
     np.testing.assert_array_equal(g["voxel"][ok], exp["voxel_ids"][ok], err_msg=label)
     if exp["neigh_list"] is not None:
@@ -45,18 +49,37 @@ def check_step(g, exp, ok, scales, dt, label):
     ps, vs = scales
     e_p = rel_err(g["pressure_term"][ok], exp["pressure_term"][ok], ps[ok] + 1e-30)
     e_v = rel_err(g["viscosity_term"][ok], exp["viscosity_term"][ok], vs[ok] + 1e-30)
-    fin = np.isfinite(exp["velocity_out"][ok])
-    vscale = (np.abs(exp["velocity_in"][ok]) +
-              np.abs(exp["result_force"][ok] / exp["density"][ok][:, None] * dt))
-    vscale = np.where(fin, vscale, 1.0)
-    e_vel = rel_err(g["velocity_out"][ok], exp["velocity_out"][ok], vscale + 1e-30)
-    e_pos = rel_err(g["position_out"][ok], exp["position_out"][ok], 1.0)
-    print(f"{label}: rho {e_rho:.1e} P {e_p:.1e} V {e_v:.1e} vel {e_vel:.1e} pos {e_pos:.1e}")
+    rho = exp["density"][ok][:, None]
+    v_ref, x_ref = exp["velocity_out"][ok], exp["position_out"][ok]
+    v_gpu, x_gpu = g["velocity_out"][ok], g["position_out"][ok]
+    for a, b, what in ((v_gpu, v_ref, "velocity"), (x_gpu, x_ref, "position")):
+        fa, fb = np.isfinite(a), np.isfinite(b)
+        assert np.array_equal(fa, fb), (label, what, "non-finite pattern", np.argwhere(fa != fb)[:5])
+    fin = np.isfinite(v_ref) & np.isfinite(x_ref) & np.isfinite(rho)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        bv = TOL_TERM * (ps[ok] + vs[ok] + np.abs(np.asarray(ext))) / rho * dt + 2.0 ** -20 * np.abs(v_ref)
+        bx = bv * dt + 2.0 ** -20 * np.maximum(np.abs(x_ref), h)
+        if collided is not None:
+            col = np.broadcast_to(collided[ok][:, None], bv.shape)
+            bv = np.where(col, 1e-3 * (np.abs(v_ref) + bv), bv)
+            bx = np.where(col, 1e-3 * np.maximum(np.abs(x_ref), h), bx)
+        nv = np.where(fin, np.abs(v_gpu - v_ref) / (bv + 1e-300), 0.0)
+        nx = np.where(fin, np.abs(x_gpu - x_ref) / (bx + 1e-300), 0.0)
+    e_vel, e_pos = float(nv.max(initial=0.0)), float(nx.max(initial=0.0))
+    print(f"{label}: rho {e_rho:.1e} P {e_p:.1e} V {e_v:.1e} vel/bound {e_vel:.2f} "
+          f"pos/bound {e_pos:.2f}")
     assert e_rho < TOL_RHO, (label, "density", e_rho)
     assert e_p < TOL_TERM, (label, "pressure", e_p)
     assert e_v < TOL_TERM, (label, "viscosity", e_v)
-    assert e_vel < TOL_VEL, (label, "velocity", e_vel)
-    assert e_pos < TOL_POS, (label, "position", e_pos)
+    assert e_vel <= 1.0, (label, "velocity", e_vel, np.unravel_index(np.argmax(nv), nv.shape))
+    assert e_pos <= 1.0, (label, "position", e_pos, np.unravel_index(np.argmax(nx), nx.shape))
+
+
+def pipe_collided(pos_in, vel_out, pos_out, dt):
+    """Particles whose position is not plain x + v dt (the wall response fired)."""
+    with np.errstate(invalid="ignore"):
+        free = np.abs(pos_in + vel_out * dt - pos_out) <= 1e-9 * np.maximum(np.abs(pos_out), 1.0)
+    return ~np.all(free, axis=1)
 
 
 @pytest.mark.parametrize("name,walk", _cases())
@@ -71,9 +94,11 @@ def test_gpu_matches_reference_golden(name, walk):
         g = run_stages(spec, pos, vel, step=s)
         ref_map = d["map_pid"][s]
         np.testing.assert_array_equal(g["sorted_pid"][ok[g["sorted_pid"]]], ref_map[ok[ref_map]])
+        nv = d["voxel_begin"].shape[1]
         if ok.all():
-            np.testing.assert_array_equal(np.where(g["count"] > 0, g["start"], -1),
+            np.testing.assert_array_equal(np.where(g["count"][:nv] > 0, g["start"][:nv], -1),
                                           d["voxel_begin"][s])
+            assert g["count"][nv] == 0     # overflow bucket empty for finite input
         # term scales from the oracle (same neighbour sets, FP64)
         spid, start, count = ref.organize(sp, ref.assign_voxels(sp, pos))
         rho = ref.density(sp, pos, spid, start, count)
@@ -81,7 +106,11 @@ def test_gpu_matches_reference_golden(name, walk):
         exp = {k: d[k][s] for k in ("voxel_ids", "neigh_list", "neigh_count", "neigh_count_uncapped",
                                      "density", "pressure_term", "viscosity_term", "result_force",
                                      "position_out", "velocity_out", "velocity_in")}
-        check_step(g, exp, ok, (ps, vs), float(d["dt"]), f"{name}/{walk}/step{s}")
+        dt = float(d["dt"])
+        col = (pipe_collided(pos, d["velocity_out"][s], d["position_out"][s], dt)
+               if str(d["mode"]) == "PIPE" else None)
+        check_step(g, exp, ok, (ps, vs), dt, f"{name}/{walk}/step{s}", ext=d["external_force"],
+                   h=float(d["inf_r"]), collided=col)
 
 
 def oracle_step_dict(spec, pos, vel, step=0):
@@ -107,9 +136,15 @@ def compare_with_oracle(spec, state, label, step=0):
     ok = in_domain(pos, spec.params.space_size)
     assert ok.all()
     np.testing.assert_array_equal(g["sorted_pid"], exp["sorted_pid"])
-    np.testing.assert_array_equal(g["count"], exp["count"])
-    np.testing.assert_array_equal(g["start"][g["count"] > 0], exp["start"][exp["count"] > 0])
-    check_step(g, exp, ok, scales, sp.dt, label)
+    nv = len(exp["count"])
+    np.testing.assert_array_equal(g["count"][:nv], exp["count"])
+    assert g["count"][nv] == 0
+    occupied = exp["count"] > 0
+    np.testing.assert_array_equal(g["start"][:nv][occupied], exp["start"][occupied])
+    col = (pipe_collided(pos, exp["velocity_out"], exp["position_out"], sp.dt)
+           if spec.mode == 'PIPE' else None)
+    check_step(g, exp, ok, scales, sp.dt, label, ext=list(sp.external_force), h=sp.inf_r,
+               collided=col)
     return g, exp
 
 
