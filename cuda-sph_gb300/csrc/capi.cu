@@ -77,6 +77,7 @@ struct SphgbCtx {
     int32_t* pidB = nullptr;
     double* pos64B = nullptr;
     float2* aux = nullptr;
+    NbrList nbr;                     // neighbour list of the step (density -> force pass)
     int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
     int32_t* big_count = nullptr;
     // bound (caller-owned) state
@@ -138,7 +139,7 @@ void free_ctx(SphgbCtx* c) {
     void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials,
-                    c->big_list, c->big_count};
+                    c->big_list, c->big_count, c->nbr.idx, c->nbr.count};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -438,11 +439,11 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
                               p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr);
     if (rc) return rc;
-    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux));
+    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
     const bool sep = c->out_pos != nullptr;
     SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB, p64B, c->vstart,
-                                c->vcount, c->scene_step, sep ? c->out_pos : c->posA,
+                                c->vcount, c->scene_step, c->nbr, sep ? c->out_pos : c->posA,
                                 sep ? c->out_vel : c->velA, sep ? c->out_pid : c->pidA,
                                 c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr,
                                 nullptr));
@@ -526,6 +527,8 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
     rc = rc ? rc : dalloc(&c->aux, N);
     rc = rc ? rc : dalloc(&c->big_list, N / kBigVoxel + 1);
     rc = rc ? rc : dalloc(&c->big_count, 1);
+    rc = rc ? rc : dalloc(&c->nbr.idx, (size_t)kListCap * N);
+    rc = rc ? rc : dalloc(&c->nbr.count, N);
     if (c->any_pipe) rc = rc ? rc : dalloc(&c->pos64B, 3 * N);
     rc = rc ? rc : dalloc(&c->d_chunks, chunks.size());
     rc = rc ? rc : dalloc(&c->d_partials, chunks.size() * 6);
@@ -841,7 +844,7 @@ int sphgb_density(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_vox
     if (ctx->n > 0 && (!d_pos_sorted || !d_rho_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
     SPHGB_CUDA(launch_density(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
-                              d_voxel_start, d_voxel_count, d_rho_out, ctx->aux));
+                              d_voxel_start, d_voxel_count, d_rho_out, ctx->aux, NbrList{}));
     return SPHGB_OK;
 }
 
@@ -881,7 +884,8 @@ int sphgb_integrate(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel
     SPHGB_CUDA(launch_integrate(L, reinterpret_cast<const float4*>(d_pos_sorted),
                                 reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
                                 ctx->aux, d_pid_sorted, d_pos64_sorted, d_voxel_start,
-                                d_voxel_count, d_scene_step, reinterpret_cast<float4*>(d_pos_out),
+                                d_voxel_count, d_scene_step, NbrList{},
+                                reinterpret_cast<float4*>(d_pos_out),
                                 reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out,
                                 reinterpret_cast<float4*>(d_force_out)));
     return SPHGB_OK;

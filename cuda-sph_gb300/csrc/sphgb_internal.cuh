@@ -350,6 +350,15 @@ __device__ inline void pipe_collide(double* p, double* v, const PipeView& P, uin
     }
 }
 
+// ---- neighbour list --------------------------------------------------------
+// Neighbours (other than self) of every particle in walk order, recorded by
+// the density pass and read by the force pass.  Column-major: idx[k * n + s].
+constexpr int kListCap = 32;
+struct NbrList {
+    int32_t* idx = nullptr;     // kListCap * n entries
+    int32_t* count = nullptr;   // n entries; -1 = more than kListCap neighbours
+};
+
 // ---- launchers (host) -----------------------------------------------------
 struct Launch {
     const SceneDev* scenes;     // device array
@@ -380,15 +389,16 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
                                const double* pos64, float4* pos_out, float4* vel_out,
                                int32_t* pid_out, double* pos64_out);
 cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
-                           const int32_t* vcount, float* rho, float2* aux);
+                           const int32_t* vcount, float* rho, float2* aux, NbrList nbr);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float2* aux, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);
 cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
                              const float* rho, const float2* aux, const int32_t* pid,
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
-                             const int32_t* scene_step, float4* pos_out, float4* vel_out,
-                             int32_t* pid_out, double* pos64_out, float4* force_out);
+                             const int32_t* scene_step, NbrList nbr, float4* pos_out,
+                             float4* vel_out, int32_t* pid_out, double* pos64_out,
+                             float4* force_out);
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, int32_t* list, int stride,
                               int32_t* n_capped, int32_t* n_uncapped);

@@ -17,11 +17,16 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // W = W_CONST (h^2 - r^2)^3 (base_kernels.py:6-9), written here as
 // W_CONST h^6 (1 - r^2/h^2)^3 so the FP32 sum stays in range for any h.
 // Also writes aux_i = (p_i / rho_i^2, 1 / rho_i) with p = K (rho - RHO_0), the
-// per-particle factors of the force pass (voxel_kernels.py:162-164, :205-208).
+// per-particle factors of the force pass (voxel_kernels.py:162-164, :205-208),
+// and, when nbr is given, the particle's neighbours other than itself in walk
+// order (the set every later kernel of the step uses), column-major
+// nbr.idx[k * n + s]; nbr.count[s] = their number, or -1 when more than
+// kListCap (the force pass then walks again).
 __global__ void __launch_bounds__(kBlock)
 k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
           int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
-          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux) {
+          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux,
+          NbrList nbr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
@@ -29,10 +34,14 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
     const float4 pi = __ldg(pos + s);
     const float inv_h2 = 1.0f / sc.h2;
     Kahan acc;
+    int others = 0;
+    int32_t* list = nbr.idx ? nbr.idx + s : nullptr;
     walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
         if (j != s) {
             const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
             acc.add(u * u * u);
+            if (list && others < kListCap) list[(size_t)others * n] = j;
+            ++others;
         }
     });
     const float r = (acc.s * sc.w_const) * sc.mass;
@@ -41,6 +50,7 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
         const float p = sc.k * (r - sc.rho0);
         aux[s] = make_float2(p / (r * r), 1.0f / r);
     }
+    if (nbr.count) nbr.count[s] = others <= kListCap ? others : -1;
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -54,9 +64,30 @@ k_aux(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, i
     aux[s] = make_float2(p / (r * r), 1.0f / r);
 }
 
+// Pressure and viscosity sums.  Compensated (Kahan) by default; kPlain sums
+// plainly, the reference's order, which is used when a factor is non-finite:
+// Kahan's compensation turns an infinite partial sum into NaN (inf - inf),
+// while the reference's plain sum stays infinite.
+template <bool kPlain>
+struct Acc {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        if (kPlain) {
+            s = __fadd_rn(s, x);
+        } else {
+            const float y = __fsub_rn(x, c);
+            const float t = __fadd_rn(s, y);
+            c = __fsub_rn(__fsub_rn(t, s), y);
+            s = t;
+        }
+    }
+};
+
+template <bool kPlain>
 struct ForceSums {
-    Kahan px, py, pz, vx, vy, vz;
-    int terms = 0;   // neighbours other than self
+    Acc<kPlain> px, py, pz, vx, vy, vz;
+    int terms = 0;      // neighbours other than self
+    bool bad = false;   // a neighbour factor was non-finite
 };
 
 // pressure_kernel (voxel_kernels.py:136-171) and viscosity_kernel (:175-211)
@@ -66,32 +97,100 @@ struct ForceSums {
 //   V_i = min(1, sum_j MASS VISC (v_j - v_i) / rho_j lap W_ij / rho_i),
 //         lap W = LAP_W_CONST (h - r)                        (base_kernels.py:24-27)
 // with (h - r) written as h (1 - r/h).
+template <bool kPlain>
+__device__ __forceinline__ void add_pair(ForceSums<kPlain>& f, const float4& vi, float a_i,
+                                         float inv_h, float gw, float lw, const float2& aj,
+                                         const float4& vj, float dx, float dy, float dz, float d2) {
+    ++f.terms;
+    if (!kPlain) f.bad |= !(fabsf(aj.x * aj.y) < INFINITY);
+    const float r = sqrtf(d2);
+    const float inv_r = 1.0f / r;
+    const float t = __fmaf_rn(-r, inv_h, 1.0f);
+    const float g = ((a_i + aj.x) * gw) * (t * t) * inv_r;
+    f.px.add(g * dx);
+    f.py.add(g * dy);
+    f.pz.add(g * dz);
+    const float l = (lw * t) * aj.y;
+    f.vx.add(l * (vj.x - vi.x));
+    f.vy.add(l * (vj.y - vi.y));
+    f.vz.add(l * (vj.z - vi.z));
+}
+
+template <bool kPlain>
 __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4& vi,
                                            float a_i, const SceneDev& sc, const WalkGeom& geom,
                                            const float4* __restrict__ pos,
                                            const float4* __restrict__ vel,
                                            const float2* __restrict__ aux,
                                            const int32_t* __restrict__ vstart,
-                                           const int32_t* __restrict__ vcount, ForceSums& f) {
+                                           const int32_t* __restrict__ vcount,
+                                           ForceSums<kPlain>& f) {
     const float inv_h = 1.0f / sc.h;
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
     walk(pi, geom, vstart, vcount, pos, geom.cap, [&](int j, float dx, float dy, float dz, float d2) {
         if (j == s) return;
-        ++f.terms;
-        const float2 aj = __ldg(aux + j);
-        const float4 vj = __ldg(vel + j);
-        const float r = sqrtf(d2);
-        const float inv_r = 1.0f / r;
-        const float t = __fmaf_rn(-r, inv_h, 1.0f);
-        const float g = ((a_i + aj.x) * gw) * (t * t) * inv_r;
-        f.px.add(g * dx);
-        f.py.add(g * dy);
-        f.pz.add(g * dz);
-        const float l = (lw * t) * aj.y;
-        f.vx.add(l * (vj.x - vi.x));
-        f.vy.add(l * (vj.y - vi.y));
-        f.vz.add(l * (vj.z - vi.z));
+        add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
     });
+}
+
+// the same sums over the neighbour list recorded by the density pass (same
+// neighbours, same order, same pair distances as the walk)
+template <bool kPlain>
+__device__ __forceinline__ void force_sums_list(const float4& pi, const float4& vi, float a_i,
+                                                const SceneDev& sc,
+                                                const float4* __restrict__ pos,
+                                                const float4* __restrict__ vel,
+                                                const float2* __restrict__ aux,
+                                                const int32_t* __restrict__ list, int n, int cnt,
+                                                ForceSums<kPlain>& f) {
+    const float inv_h = 1.0f / sc.h;
+    const float gw = sc.grad_w_const, lw = sc.lap_w_const;
+#pragma unroll 4
+    for (int k = 0; k < cnt; ++k) {
+        const int j = __ldg(list + (size_t)k * n);
+        const float4 pj = __ldg(pos + j);
+        const float dx = __fsub_rn(pi.x, pj.x);
+        const float dy = __fsub_rn(pi.y, pj.y);
+        const float dz = __fsub_rn(pi.z, pj.z);
+        float d2 = __fmul_rn(dx, dx);
+        d2 = __fmaf_rn(dy, dy, d2);
+        d2 = __fmaf_rn(dz, dz, d2);
+        add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
+    }
+}
+
+struct Forces {
+    float p[3], v[3];   // pressure term, viscosity sum (before the 1/rho_i scale)
+    int terms;
+};
+
+// Kahan sums, redone plainly when a factor of particle i or of a neighbour
+// is non-finite (a particle of density 0).  With a neighbour list (cnt >= 0)
+// the neighbours come from it, else from a fresh walk.
+__device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float4& vi,
+                                            const float2& ai, const SceneDev& sc,
+                                            const float4* __restrict__ pos,
+                                            const float4* __restrict__ vel,
+                                            const float2* __restrict__ aux,
+                                            const int32_t* __restrict__ vstart,
+                                            const int32_t* __restrict__ vcount,
+                                            const int32_t* __restrict__ list, int n, int cnt) {
+    Forces out;
+    bool plain = !(fabsf(ai.x * ai.y) < INFINITY);
+    if (!plain) {
+        ForceSums<false> f;
+        if (cnt >= 0) force_sums_list<false>(pi, vi, ai.x, sc, pos, vel, aux, list, n, cnt, f);
+        else force_sums<false>(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+        out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
+        plain = f.bad;
+    }
+    if (plain) {
+        ForceSums<true> f;
+        if (cnt >= 0) force_sums_list<true>(pi, vi, ai.x, sc, pos, vel, aux, list, n, cnt, f);
+        else force_sums<true>(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+        out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
+    }
+    return out;
 }
 
 __device__ __forceinline__ float clamp1(float x) { return x < 1.0f ? x : 1.0f; }  // min(1, x)
@@ -99,8 +198,8 @@ __device__ __forceinline__ float clamp1(float x) { return x < 1.0f ? x : 1.0f; }
 // viscosity term of one component: the reference multiplies every neighbour
 // term by MASS * VISC / rho_i (voxel_kernels.py:207-208), so with no
 // neighbour terms the sum is 0 even when rho_i is 0
-__device__ __forceinline__ float visc_term(const ForceSums& f, float sum, float vscale) {
-    return clamp1(f.terms ? sum * vscale : 0.0f);
+__device__ __forceinline__ float visc_term(const Forces& f, int a, float vscale) {
+    return clamp1(f.terms ? f.v[a] * vscale : 0.0f);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -115,12 +214,11 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
     const float4 pi = __ldg(pos + s);
     const float4 vi = __ldg(vel + s);
     const float2 ai = __ldg(aux + s);
-    ForceSums f;
-    force_sums(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+    const Forces f = forces_of(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount, nullptr, n, -1);
     const float vscale = sc.mass * sc.visc * ai.y;
-    pressure[s] = make_float4(f.px.s, f.py.s, f.pz.s, 0.0f);
-    viscosity[s] = make_float4(visc_term(f, f.vx.s, vscale), visc_term(f, f.vy.s, vscale),
-                               visc_term(f, f.vz.s, vscale), 0.0f);
+    pressure[s] = make_float4(f.p[0], f.p[1], f.p[2], 0.0f);
+    viscosity[s] = make_float4(visc_term(f, 0, vscale), visc_term(f, 1, vscale),
+                               visc_term(f, 2, vscale), 0.0f);
 }
 
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
@@ -133,7 +231,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             const float2* __restrict__ aux, const int32_t* __restrict__ pid,
             const double* __restrict__ pos64, const int32_t* __restrict__ vstart,
             const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
-            float4* __restrict__ pos_out, float4* __restrict__ vel_out,
+            NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
             float4* __restrict__ force_out) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,14 +242,14 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const float4 vi = __ldg(vel + s);
     const float2 ai = __ldg(aux + s);
     const float rho_i = __ldg(rho + s);
-    ForceSums f;
-    force_sums(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+    const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
+    const Forces f = forces_of(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount,
+                               nbr.idx ? nbr.idx + s : nullptr, n, cnt);
     const float vscale = sc.mass * sc.visc * ai.y;
     // result_force = ext + -P + V (base_kernels.py:46-52)
     float F[3];
-    F[0] = (sc.ext[0] + -f.px.s) + visc_term(f, f.vx.s, vscale);
-    F[1] = (sc.ext[1] + -f.py.s) + visc_term(f, f.vy.s, vscale);
-    F[2] = (sc.ext[2] + -f.pz.s) + visc_term(f, f.vz.s, vscale);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) F[a] = (sc.ext[a] + -f.p[a]) + visc_term(f, a, vscale);
     float v[3] = {vi.x, vi.y, vi.z};
 #pragma unroll
     for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
@@ -220,10 +318,10 @@ k_neighbours(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
 }  // namespace
 
 cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
-                           const int32_t* vcount, float* rho, float2* aux) {
+                           const int32_t* vcount, float* rho, float2* aux, NbrList nbr) {
     if (L.n == 0) return cudaSuccess;
     k_density<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                         vstart, vcount, rho, aux);
+                                                         vstart, vcount, rho, aux, nbr);
     return cudaGetLastError();
 }
 
@@ -247,12 +345,13 @@ cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
 cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
                              const float* rho, const float2* aux, const int32_t* pid,
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
-                             const int32_t* scene_step, float4* pos_out, float4* vel_out,
-                             int32_t* pid_out, double* pos64_out, float4* force_out) {
+                             const int32_t* scene_step, NbrList nbr, float4* pos_out,
+                             float4* vel_out, int32_t* pid_out, double* pos64_out,
+                             float4* force_out) {
     if (L.n == 0) return cudaSuccess;
     k_integrate<<<blocks_for(L.n), kBlock, 0, L.stream>>>(
         L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
-        vcount, scene_step, pos_out, vel_out, pid_out, pos64_out, force_out);
+        vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
     return cudaGetLastError();
 }
 

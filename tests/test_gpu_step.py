@@ -1,0 +1,123 @@
+"""The fused, device-resident step (SceneBatch / sphgb_ctx_step): identical to
+the stage-by-stage path, to its CUDA-graph replay, alone or batched, and
+within FP32 tolerance of the oracle through the host-buffer entry point."""
+import numpy as np
+import pytest
+
+from gpu_util import run_stages, torch_cuda
+from oracle import ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    from sphgb import scenes
+    return {
+        "config0": scenes.config0(),
+        "pipe": scenes.pipe_flow(n=20_000, seed=11, h=0.02 * (262_144 / 20_000) ** (1 / 3)),
+        "uncapped": scenes.box_dam_break(nx=10, ny=20, nz=10, max_neighbours=0, seed=4),
+        "truncated": scenes.box_dam_break(nx=10, ny=20, nz=10, box=(0.7, 0.7, 0.7),
+                                          walk_dims='truncated', seed=5),
+    }
+
+
+@pytest.mark.parametrize("name", ["config0", "pipe", "uncapped", "truncated"])
+def test_fused_step_bit_identical_to_stages(name):
+    """The fused step reads the density pass's neighbour list; the stage path
+    walks again.  Same neighbours, order and arithmetic: identical bits."""
+    torch_cuda()
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()[name]
+    g = run_stages(spec, st.position, st.velocity, step=0)
+    b = SceneBatch([spec])
+    b.load_states([st])
+    b.step(1)
+    out = b.states()[0]
+    np.testing.assert_array_equal(out.density, g["density"])
+    np.testing.assert_array_equal(out.velocity, g["velocity_out"])
+    np.testing.assert_array_equal(out.position, g["position_out"])
+    b.close()
+
+
+def test_graph_replay_equals_eager():
+    torch_cuda()
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()["config0"]
+    outs = []
+    for use_graph in (False, True):
+        b = SceneBatch([spec])
+        b.load_states([st])
+        for _ in range(3):
+            b.step(2, use_graph=use_graph)
+        outs.append(b.states()[0])
+        b.close()
+    for f in ("position", "velocity", "density"):
+        np.testing.assert_array_equal(getattr(outs[0], f), getattr(outs[1], f))
+
+
+def test_batched_scenes_identical_to_alone():
+    """Scenes advanced together give bit-identical states and conservation sums
+    to each scene advanced alone (different constants, modes and sizes)."""
+    torch_cuda()
+    from sphgb import scenes
+    from sphgb.device import SceneBatch
+    picks = [_scenes()["config0"], _scenes()["pipe"],
+             scenes.box_dam_break(nx=6, ny=12, nz=6, spacing=0.03, h=0.0675, mass=0.027, seed=9,
+                                  gravity=(1.0, -9.0, 3.0))]
+    together = SceneBatch([p[0] for p in picks])
+    together.load_states([p[1] for p in picks])
+    together.step(4, use_graph=True)
+    t_states = together.states()
+    t_cons = together.conservation()
+    for k, (spec, st) in enumerate(picks):
+        alone = SceneBatch([spec])
+        alone.load_states([st])
+        alone.step(4, use_graph=True)
+        a = alone.states()[0]
+        for f in ("position", "velocity", "density"):
+            np.testing.assert_array_equal(getattr(a, f), getattr(t_states[k], f), err_msg=f"{k} {f}")
+        np.testing.assert_array_equal(alone.conservation()[0], t_cons[k])
+        alone.close()
+    together.close()
+
+
+def test_host_entry_matches_oracle():
+    """sphgb_compute_next_state_host (FP64 AoS host buffers in and out) against
+    the oracle's step on the same input."""
+    torch_cuda()
+    from sphgb.strategies import GB300SPHStrategy
+    spec, st = _scenes()["config0"]
+    strat = GB300SPHStrategy(spec.params, constants=spec.constants, mode=spec.mode)
+    out = strat.compute_next_state(st)
+    sp = ref.params_from_spec(spec)
+    pos, vel, rho = ref.step(sp, st.position, st.velocity, step_index=0)
+    assert np.max(np.abs(out.density - rho) / rho) < 1e-5
+    assert np.max(np.abs(out.position - pos)) < 1e-6
+    # velocities: cancellation in F makes a relative bound meaningless; bound by
+    # the term scale like the stage tests (here via the step's own magnitude)
+    assert np.max(np.abs(out.velocity - vel)) < 2e-4 * (np.abs(vel).max() + 1.0)
+    # the strategy keeps the reference's attributes
+    assert strat.old_state is st and strat.new_state is out and strat.dt == 1 / spec.params.fps
+
+
+def test_trajectory_config0_200_steps():
+    """200 free-running steps of the 8,192-particle dam break against the FP64
+    oracle: report divergence (the capped walk makes the reference's dynamics
+    chaotic: one neighbour entering at r ~ h displaces the 32nd)."""
+    torch_cuda()
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()["config0"]
+    sp = ref.params_from_spec(spec)
+    b = SceneBatch([spec])
+    b.load_states([st])
+    pos, vel = st.position.copy(), st.velocity.copy()
+    for k in range(200):
+        pos, vel, rho = ref.step(sp, pos, vel, step_index=k)
+        b.step(1)
+        if k + 1 in (1, 10, 50, 100, 200):
+            g = b.states()[0]
+            dx = np.linalg.norm(g.position - pos, axis=1)
+            print(f"step {k + 1}: |dx| median {np.median(dx):.2e} p99 {np.quantile(dx, 0.99):.2e} "
+                  f"max {dx.max():.2e}; mean rho gpu {g.density.mean():.3f} oracle {rho.mean():.3f}")
+            assert np.isfinite(g.position).all()
+    b.close()
