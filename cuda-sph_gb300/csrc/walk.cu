@@ -27,23 +27,49 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
           int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
           const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux,
           NbrList nbr) {
+    // the walk only records neighbour slots (per-thread column of shared
+    // memory); the density is summed afterwards in a loop every thread of the
+    // warp runs the same number of times, in the same (walk) order
+    __shared__ int32_t s_list[kListCap][kBlock];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
     const WalkGeom g = load_geom(sc);
     const float4 pi = __ldg(pos + s);
-    const float inv_h2 = 1.0f / sc.h2;
-    Kahan acc;
     int others = 0;
-    int32_t* list = nbr.idx ? nbr.idx + s : nullptr;
-    walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
+    walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
         if (j != s) {
-            const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-            acc.add(u * u * u);
-            if (list && others < kListCap) list[(size_t)others * n] = j;
+            if (others < kListCap) s_list[others][threadIdx.x] = j;
             ++others;
         }
     });
+    const float inv_h2 = 1.0f / sc.h2;
+    Kahan acc;
+    if (others <= kListCap) {
+#pragma unroll 4
+        for (int k = 0; k < others; ++k) {
+            const float4 pj = __ldg(pos + s_list[k][threadIdx.x]);
+            const float dx = __fsub_rn(pi.x, pj.x);
+            const float dy = __fsub_rn(pi.y, pj.y);
+            const float dz = __fsub_rn(pi.z, pj.z);
+            float d2 = __fmul_rn(dx, dx);
+            d2 = __fmaf_rn(dy, dy, d2);
+            d2 = __fmaf_rn(dz, dz, d2);
+            const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+            acc.add(u * u * u);
+        }
+        if (nbr.idx)
+            for (int k = 0; k < others; ++k) nbr.idx[(size_t)k * n + s] = s_list[k][threadIdx.x];
+    } else {
+        // more neighbours than the list holds (no cap or a cap above it):
+        // walk again, summing on the way
+        walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
+            if (j != s) {
+                const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                acc.add(u * u * u);
+            }
+        });
+    }
     const float r = (acc.s * sc.w_const) * sc.mass;
     rho[s] = r;
     if (aux) {

@@ -102,8 +102,14 @@ def test_host_entry_matches_oracle():
 
 def test_trajectory_config0_200_steps():
     """200 free-running steps of the 8,192-particle dam break against the FP64
-    oracle: report divergence (the capped walk makes the reference's dynamics
-    chaotic: one neighbour entering at r ~ h displaces the 32nd)."""
+    oracle.  The reference's capped walk makes the dynamics chaotic (a pair
+    crossing r = h changes which particle is the 32nd neighbour), so FP32 and
+    FP64 trajectories separate over time; the tolerances are per phase:
+      step 10        every particle within 1e-5 of the oracle
+      step 50        99 % of particles within 1e-4, median within 1e-6
+      step 100       median within 1e-5
+      every check    mean density within 1 %, non-finite particles <= 1 %
+    """
     torch_cuda()
     from sphgb.device import SceneBatch
     spec, st = _scenes()["config0"]
@@ -111,13 +117,27 @@ def test_trajectory_config0_200_steps():
     b = SceneBatch([spec])
     b.load_states([st])
     pos, vel = st.position.copy(), st.velocity.copy()
+    n = len(pos)
     for k in range(200):
         pos, vel, rho = ref.step(sp, pos, vel, step_index=k)
         b.step(1)
-        if k + 1 in (1, 10, 50, 100, 200):
-            g = b.states()[0]
-            dx = np.linalg.norm(g.position - pos, axis=1)
-            print(f"step {k + 1}: |dx| median {np.median(dx):.2e} p99 {np.quantile(dx, 0.99):.2e} "
-                  f"max {dx.max():.2e}; mean rho gpu {g.density.mean():.3f} oracle {rho.mean():.3f}")
-            assert np.isfinite(g.position).all()
+        step = k + 1
+        if step not in (1, 10, 50, 100, 150, 200):
+            continue
+        g = b.states()[0]
+        fin = np.isfinite(g.position).all(1) & np.isfinite(pos).all(1)
+        dx = np.linalg.norm(g.position - pos, axis=1)[fin]
+        med, p99, mx = np.median(dx), np.quantile(dx, 0.99), dx.max()
+        drho = abs(g.density.mean() - rho.mean()) / rho.mean()
+        print(f"step {step}: |dx| median {med:.2e} p99 {p99:.2e} max {mx:.2e}; "
+              f"mean rho rel diff {drho:.1e}; non-finite gpu {n - np.isfinite(g.position).all(1).sum()} "
+              f"oracle {n - np.isfinite(pos).all(1).sum()}")
+        assert drho < 1e-2
+        assert (~fin).sum() <= 0.01 * n
+        if step <= 10:
+            assert mx < 1e-5
+        elif step == 50:
+            assert p99 < 1e-4 and med < 1e-6
+        elif step == 100:
+            assert med < 1e-5
     b.close()
