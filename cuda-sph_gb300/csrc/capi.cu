@@ -114,6 +114,7 @@ struct SphgbCtx {
         L.n = n;
         L.v_total = v_total;
         L.pipe = d_pipe;
+        L.pipe_scenes = any_pipe;
         L.stream = st;
         return L;
     }

@@ -367,6 +367,7 @@ struct Launch {
     int n;                      // particles (all scenes)
     int v_total;                // voxels (all scenes)
     const double* pipe;         // device pipe table (may be null)
+    bool pipe_scenes;           // some scene is in pipe mode
     cudaStream_t stream;
 };
 

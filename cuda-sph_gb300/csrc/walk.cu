@@ -249,7 +249,9 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
 
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
 // (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
-// state into the *_out buffers at the same slot.
+// state into the *_out buffers at the same slot.  kPipe = false is the
+// instantiation for contexts without pipe scenes (no FP64 code).
+template <bool kPipe>
 __global__ void __launch_bounds__(kBlock)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
@@ -280,7 +282,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
 #pragma unroll
     for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
     const int p_id = __ldg(pid + s);
-    if (sc.mode == 0) {
+    if (!kPipe || sc.mode == 0) {
         float x[3] = {pi.x, pi.y, pi.z};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -291,12 +293,12 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             if (bounced) v[a] = -v[a] * sc.damp;
         }
         pos_out[s] = make_float4(x[0], x[1], x[2], 0.0f);
-        if (pos64_out) {
+        if (kPipe && pos64_out) {
             pos64_out[3 * s + 0] = x[0];
             pos64_out[3 * s + 1] = x[1];
             pos64_out[3 * s + 2] = x[2];
         }
-    } else {
+    } else if (kPipe) {
         // pipe flow: FP64 position accumulator and FP64 wall response
         double x[3], vd[3];
 #pragma unroll
@@ -375,9 +377,14 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
                              float4* force_out) {
     if (L.n == 0) return cudaSuccess;
-    k_integrate<<<blocks_for(L.n), kBlock, 0, L.stream>>>(
-        L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
-        vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
+    if (L.pipe_scenes)
+        k_integrate<true><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
+    else
+        k_integrate<false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
     return cudaGetLastError();
 }
 
