@@ -79,7 +79,8 @@ struct SphgbCtx {
     float2* aux = nullptr;
     NbrList nbr;                     // neighbour list of the step (density -> force pass)
     int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
-    int32_t* big_count = nullptr;
+    int32_t* big_count = nullptr;     // counters[0]: big voxels, counters[1]: density tasks
+    int2* tasks = nullptr;             // (voxel, first slot) per run of <= 32 slots
     // bound (caller-owned) state
     float4* posA = nullptr;
     float4* velA = nullptr;
@@ -140,7 +141,7 @@ void free_ctx(SphgbCtx* c) {
     void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials,
-                    c->big_list, c->big_count, c->nbr.idx, c->nbr.count};
+                    c->big_list, c->big_count, c->nbr.idx, c->nbr.count, c->tasks};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -412,10 +413,10 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const float4* vel,
                      const int32_t* pid, const double* pos64, float4* pos_o, float4* vel_o,
                      int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
-                     cudaEvent_t* ev = nullptr) {
+                     cudaEvent_t* ev = nullptr, bool with_tasks = false) {
     cudaStream_t st = L.stream;
     if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * c->v_total, st));
-    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, sizeof(int32_t), st));
+    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 2 * sizeof(int32_t), st));
     SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, c->n_tiles));
@@ -425,7 +426,8 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
     SPHGB_CUDA(launch_sort_big(L, c->big_list, c->big_count, vstart, vcount, c->tmp_pid));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[2], st));
     SPHGB_CUDA(launch_rank_gather(L, c->cell, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
-                                  pos_o, vel_o, pid_o, pos64_o));
+                                  pos_o, vel_o, pid_o, pos64_o, with_tasks ? c->tasks : nullptr,
+                                  with_tasks ? c->big_count + 1 : nullptr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[3], st));
     return SPHGB_OK;
 }
@@ -438,9 +440,10 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
-                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr);
+                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
     if (rc) return rc;
-    SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
+    SPHGB_CUDA(launch_density_wc(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
+                                 c->tasks, c->big_count + 1));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
     const bool sep = c->out_pos != nullptr;
     SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB, p64B, c->vstart,
@@ -527,7 +530,8 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
     rc = rc ? rc : dalloc(&c->pidB, N);
     rc = rc ? rc : dalloc(&c->aux, N);
     rc = rc ? rc : dalloc(&c->big_list, N / kBigVoxel + 1);
-    rc = rc ? rc : dalloc(&c->big_count, 1);
+    rc = rc ? rc : dalloc(&c->big_count, 2);
+    rc = rc ? rc : dalloc(&c->tasks, N);
     rc = rc ? rc : dalloc(&c->nbr.idx, (size_t)kListCap * N);
     rc = rc ? rc : dalloc(&c->nbr.count, N);
     if (c->any_pipe) rc = rc ? rc : dalloc(&c->pos64B, 3 * N);

@@ -233,7 +233,8 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
               const int32_t* __restrict__ vcount, const float4* __restrict__ pos,
               const float4* __restrict__ vel, const double* __restrict__ pos64,
               float4* __restrict__ pos_out, float4* __restrict__ vel_out,
-              int32_t* __restrict__ pid_out, double* __restrict__ pos64_out) {
+              int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
+              int2* __restrict__ tasks, int32_t* __restrict__ task_count) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int vid = cell[s];
@@ -252,6 +253,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
         r = lo;
     }
     const int d = st + r;
+    if (tasks && (r & 31) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
     pid_out[d] = p;
     pos_out[d] = __ldg(pos + s);
     vel_out[d] = __ldg(vel + s);
@@ -306,11 +308,13 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
                                const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,
                                const double* pos64, float4* pos_out, float4* vel_out,
-                               int32_t* pid_out, double* pos64_out) {
+                               int32_t* pid_out, double* pos64_out, int2* tasks,
+                               int32_t* task_count) {
     if (L.n == 0) return cudaSuccess;
     k_rank_gather<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart,
                                                              vcount, pos, vel, pos64, pos_out,
-                                                             vel_out, pid_out, pos64_out);
+                                                             vel_out, pid_out, pos64_out, tasks,
+                                                             task_count);
     return cudaGetLastError();
 }
 

@@ -384,13 +384,20 @@ cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* 
 constexpr int kBigVoxel = 64;
 cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
+// tasks (optional): one (voxel, first slot) entry per run of up to 32 sorted
+// slots of a voxel, appended at task_count
 cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
                                const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,
                                const double* pos64, float4* pos_out, float4* vel_out,
-                               int32_t* pid_out, double* pos64_out);
+                               int32_t* pid_out, double* pos64_out, int2* tasks = nullptr,
+                               int32_t* task_count = nullptr);
 cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
                            const int32_t* vcount, float* rho, float2* aux, NbrList nbr);
+// the step's density pass: one warp per task (<= 32 particles of one voxel)
+cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
+                              const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
+                              const int2* tasks, const int32_t* task_count);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float2* aux, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);

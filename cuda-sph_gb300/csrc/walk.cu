@@ -22,24 +22,20 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // order (the set every later kernel of the step uses), column-major
 // nbr.idx[k * n + s]; nbr.count[s] = their number, or -1 when more than
 // kListCap (the force pass then walks again).
-__global__ void __launch_bounds__(kBlock)
-k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
-          int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
-          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux,
-          NbrList nbr) {
-    // the walk only records neighbour slots (per-thread column of shared
-    // memory); the density is summed afterwards in a loop every thread of the
-    // warp runs the same number of times, in the same (walk) order
-    __shared__ int32_t s_list[kListCap][kBlock];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+// One particle's density by a thread-private walk: the walk records neighbour
+// slots in row[k * stride] (k < kListCap), the sum runs afterwards in walk
+// order; with more neighbours than that the walk is repeated, summing.
+__device__ __forceinline__ void density_one(int s, const float4& pi, const SceneDev& sc,
+                                            const float4* __restrict__ pos,
+                                            const int32_t* __restrict__ vstart,
+                                            const int32_t* __restrict__ vcount, int n,
+                                            float* __restrict__ rho, float2* __restrict__ aux,
+                                            const NbrList& nbr, int32_t* row, int stride) {
     const WalkGeom g = load_geom(sc);
-    const float4 pi = __ldg(pos + s);
     int others = 0;
     walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
         if (j != s) {
-            if (others < kListCap) s_list[others][threadIdx.x] = j;
+            if (others < kListCap) row[others * stride] = j;
             ++others;
         }
     });
@@ -48,7 +44,7 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
     if (others <= kListCap) {
 #pragma unroll 4
         for (int k = 0; k < others; ++k) {
-            const float4 pj = __ldg(pos + s_list[k][threadIdx.x]);
+            const float4 pj = __ldg(pos + row[k * stride]);
             const float dx = __fsub_rn(pi.x, pj.x);
             const float dy = __fsub_rn(pi.y, pj.y);
             const float dz = __fsub_rn(pi.z, pj.z);
@@ -59,7 +55,7 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
             acc.add(u * u * u);
         }
         if (nbr.idx)
-            for (int k = 0; k < others; ++k) nbr.idx[(size_t)k * n + s] = s_list[k][threadIdx.x];
+            for (int k = 0; k < others; ++k) nbr.idx[(size_t)k * n + s] = row[k * stride];
     } else {
         // more neighbours than the list holds (no cap or a cap above it):
         // walk again, summing on the way
@@ -77,6 +73,159 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
         aux[s] = make_float2(p / (r * r), 1.0f / r);
     }
     if (nbr.count) nbr.count[s] = others <= kListCap ? others : -1;
+}
+
+// thread per particle (used by the stage entry points and as the reference
+// path of the warp-cooperative kernel below)
+__global__ void __launch_bounds__(kBlock)
+k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
+          int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
+          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux,
+          NbrList nbr) {
+    __shared__ int32_t s_list[kListCap][kBlock];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    density_one(s, __ldg(pos + s), sc, pos, vstart, vcount, n, rho, aux, nbr,
+                &s_list[0][threadIdx.x], kBlock);
+}
+
+// Warp-cooperative density pass of the step.  One warp per task: up to 32
+// particles of one voxel (tasks listed by the rank-gather).  The 27 walk
+// voxels of that voxel are laid end to end in walk order; each batch of 32
+// candidates is loaded coalesced, one per lane, and every home particle is
+// tested against the whole batch at once: a ballot gives its accepted
+// candidates in walk order and popc ranks them against the cap, so the
+// accepted set is exactly the reference's first MAX_NEIGHBOURS (self
+// included).  Then each home particle sums its density over that list in
+// walk order with the same arithmetic as density_one: the results are
+// bit-identical to the thread-per-particle kernel.
+constexpr int kWcWarps = 8;
+constexpr int kWcList = kListCap;       // accepted neighbours per particle, self included
+
+struct WcShared {
+    float4 home[32];
+    int32_t list[32][kWcList];
+    int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
+    int32_t st[27];     // first slot of each walk voxel
+};
+
+__global__ void __launch_bounds__(kWcWarps * 32)
+k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+             int n_scenes, int n, const float4* __restrict__ pos,
+             const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+             float* __restrict__ rho, float2* __restrict__ aux, NbrList nbr,
+             const int2* __restrict__ tasks, const int32_t* __restrict__ task_count) {
+    __shared__ WcShared sh[kWcWarps];
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    WcShared& S = sh[threadIdx.x >> 5];
+    const unsigned lt = (1u << lane) - 1u;
+    const int n_tasks = *task_count;
+    for (int t = blockIdx.x * kWcWarps + (threadIdx.x >> 5); t < n_tasks;
+         t += gridDim.x * kWcWarps) {
+        const int2 task = tasks[t];
+        const int vid = task.x, d0 = task.y;
+        const SceneDev& sc = scenes[scene_of(d0, pbegin, n_scenes)];
+        const int vst = __ldg(vstart + vid), vc = __ldg(vcount + vid);
+        const int c_t = min(32, vst + vc - d0);
+        const int s = d0 + lane;
+        const bool home = lane < c_t;
+        const float4 pi = home ? __ldg(pos + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int local = vid - sc.v_begin;
+        const int cap = sc.cap;
+        if (local == sc.v_count || cap > kListCap) {
+            // overflow bucket (non-finite positions) or a cap beyond the shared
+            // list: thread-private walk per particle
+            if (home) density_one(s, pi, sc, pos, vstart, vcount, n, rho, aux, nbr, &S.list[lane][0], 1);
+            __syncwarp();
+            continue;
+        }
+        if (home) S.home[lane] = pi;
+        // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
+        int ck = 0, stk = 0;
+        if (lane < 27) {
+            const int D0 = sc.dims[0], D1 = sc.dims[1];
+            const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
+            const int vx = local % D0, vy = (local / D0) % D1, vz = local / (D0 * D1);
+            const int nx = vx + lane / 9 - 1, ny = vy + (lane / 3) % 3 - 1, nz = vz + lane % 3 - 1;
+            if (nx >= 0 && nx < w0 && ny >= 0 && ny < w1 && nz >= 0 && nz < w2) {
+                const int id = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
+                ck = __ldg(vcount + id);
+                stk = __ldg(vstart + id);
+            }
+        }
+        int incl = ck;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane < 27) { S.P[lane] = incl - ck; S.st[lane] = stk; }
+        const int M = __shfl_sync(full, incl, 26);
+        __syncwarp();
+        const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
+        const double h_d = sc.h_d;
+        int cnt = 0;    // lane i: accepted candidates of home particle i so far
+        for (int b0 = 0; b0 < M; b0 += 32) {
+            const int q = b0 + lane;
+            float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
+            int sj = -1;
+            if (q < M) {
+                int lo = 0, hi = 26;            // last walk voxel with P <= q
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (S.P[mid] <= q) lo = mid; else hi = mid - 1;
+                }
+                sj = S.st[lo] + (q - S.P[lo]);
+                pj = __ldg(pos + sj);
+            }
+            bool active = false;
+            for (int i = 0; i < c_t; ++i) {
+                const int ci = __shfl_sync(full, cnt, i);
+                if (ci >= cap) continue;
+                active = true;
+                const float4 ph = S.home[i];
+                float dx, dy, dz, d2;
+                const bool acc = q < M && within(ph, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2);
+                const unsigned mask = __ballot_sync(full, acc);
+                const int rank = ci + __popc(mask & lt);
+                if (acc && rank < cap) S.list[i][rank] = sj;
+                if (lane == i) cnt = ci + __popc(mask);
+            }
+            if (!active) break;
+        }
+        __syncwarp();
+        if (home) {
+            const int na = min(cnt, cap);
+            const float inv_h2 = 1.0f / sc.h2;
+            Kahan acc;
+            int others = 0;
+            for (int k = 0; k < na; ++k) {
+                const int j = S.list[lane][k];
+                if (j == s) continue;
+                const float4 pj = __ldg(pos + j);
+                const float dx = __fsub_rn(pi.x, pj.x);
+                const float dy = __fsub_rn(pi.y, pj.y);
+                const float dz = __fsub_rn(pi.z, pj.z);
+                float d2 = __fmul_rn(dx, dx);
+                d2 = __fmaf_rn(dy, dy, d2);
+                d2 = __fmaf_rn(dz, dz, d2);
+                const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                acc.add(u * u * u);
+                if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
+                ++others;
+            }
+            const float r = (acc.s * sc.w_const) * sc.mass;
+            rho[s] = r;
+            if (aux) {
+                const float p = sc.k * (r - sc.rho0);
+                aux[s] = make_float2(p / (r * r), 1.0f / r);
+            }
+            if (nbr.count) nbr.count[s] = others;
+        }
+        __syncwarp();
+    }
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -350,6 +499,20 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vs
     if (L.n == 0) return cudaSuccess;
     k_density<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                          vstart, vcount, rho, aux, nbr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
+                              const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
+                              const int2* tasks, const int32_t* task_count) {
+    if (L.n == 0) return cudaSuccess;
+    // persistent grid: 6 blocks of 8 warps per SM, warps stride over the tasks
+    int blocks = (L.n + 31) / 32;
+    if (blocks > 152 * 6) blocks = 152 * 6;
+    blocks = (blocks + kWcWarps - 1) / kWcWarps;
+    k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
+                                                         vstart, vcount, rho, aux, nbr, tasks,
+                                                         task_count);
     return cudaGetLastError();
 }
 
