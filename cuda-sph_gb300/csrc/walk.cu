@@ -105,7 +105,7 @@ constexpr int kWcList = kListCap;       // accepted neighbours per particle, sel
 
 struct WcShared {
     float4 home[32];
-    int32_t list[32][kWcList];
+    int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
     int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
     int32_t st[27];     // first slot of each walk voxel
 };
@@ -180,20 +180,29 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                 sj = S.st[lo] + (q - S.P[lo]);
                 pj = __ldg(pos + sj);
             }
-            bool active = false;
-            for (int i = 0; i < c_t; ++i) {
+            // home particles still below the cap
+            unsigned todo = __ballot_sync(full, home && cnt < cap);
+            if (!todo) break;
+            while (todo) {
+                const int i = __ffs(todo) - 1;
+                todo &= todo - 1;
                 const int ci = __shfl_sync(full, cnt, i);
-                if (ci >= cap) continue;
-                active = true;
                 const float4 ph = S.home[i];
-                float dx, dy, dz, d2;
-                const bool acc = q < M && within(ph, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2);
+                const float dx = __fsub_rn(ph.x, pj.x);
+                const float dy = __fsub_rn(ph.y, pj.y);
+                const float dz = __fsub_rn(ph.z, pj.z);
+                float d2 = __fmul_rn(dx, dx);
+                d2 = __fmaf_rn(dy, dy, d2);
+                d2 = __fmaf_rn(dz, dz, d2);
+                bool acc = q < M && d2 < h2_lo;
+                const bool band = q < M && d2 >= h2_lo && d2 <= h2_hi;
+                if (__any_sync(full, band))
+                    if (band) acc = within_exact(ph.x, ph.y, ph.z, pj.x, pj.y, pj.z, h_d);
                 const unsigned mask = __ballot_sync(full, acc);
                 const int rank = ci + __popc(mask & lt);
                 if (acc && rank < cap) S.list[i][rank] = sj;
                 if (lane == i) cnt = ci + __popc(mask);
             }
-            if (!active) break;
         }
         __syncwarp();
         if (home) {
@@ -401,7 +410,7 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
 // state into the *_out buffers at the same slot.  kPipe = false is the
 // instantiation for contexts without pipe scenes (no FP64 code).
 template <bool kPipe>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, kPipe ? 1 : 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
             const float4* __restrict__ vel, const float* __restrict__ rho,
@@ -506,10 +515,9 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t*
                               const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
                               const int2* tasks, const int32_t* task_count) {
     if (L.n == 0) return cudaSuccess;
-    // persistent grid: 6 blocks of 8 warps per SM, warps stride over the tasks
-    int blocks = (L.n + 31) / 32;
-    if (blocks > 152 * 6) blocks = 152 * 6;
-    blocks = (blocks + kWcWarps - 1) / kWcWarps;
+    // persistent grid: up to 4 blocks of 8 warps per SM, warps stride over the tasks
+    int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
+    if (blocks > 152 * 4) blocks = 152 * 4;
     k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                          vstart, vcount, rho, aux, nbr, tasks,
                                                          task_count);
