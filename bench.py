@@ -186,10 +186,10 @@ def measured_peak_hbm():
 
 def committed_traffic(stage):
     """DRAM bytes per launch of a stage's kernel from the committed ncu summary
-    (profiles/<kernel>_config2.txt, line 'traffic_bytes_per_launch: X')."""
-    names = {"force_integrate": "k_integrate", "density": "k_density",
+    (profiles/<kernel>_config2.md, line 'traffic_bytes_per_launch: X')."""
+    names = {"force_integrate": "k_integrate", "density": "k_density_wc",
              "rank_gather": "k_rank_gather"}
-    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_config2.txt")
+    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_config2.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
