@@ -13,6 +13,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -944,3 +945,117 @@ int sphgb_philox_uniform(uint64_t seed, const int32_t* d_pid, int n, int step, i
 }
 
 }  // extern "C"
+
+// ---- voxel organisation without allocation --------------------------------
+//
+// For callers that cannot allocate device memory (cudaMalloc is forbidden in
+// their process, or they run inside a host allocator of their own and may not
+// add allocations behind its back): the same kernels as
+// sphgb_organize_voxels, with every scratch buffer in one file-scope
+// __device__ array of fixed size.  Each GPU that loads this library holds the
+// array (about 3.2 MB) until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxParticles = 262144;
+constexpr int kNoAllocMaxVoxels = 4194304;   // voxel-table entries, overflow entry included
+constexpr int kNoAllocMaxTiles = (kNoAllocMaxVoxels + 4095) / 4096;
+
+struct NoAllocScratch {
+    SceneDev scene;
+    int32_t pbegin[2];
+    int32_t counters[2];
+    int32_t tile_sums[kNoAllocMaxTiles];
+    int32_t cell[kNoAllocMaxParticles];
+    int32_t slot[kNoAllocMaxParticles];
+    int32_t tmp_pid[kNoAllocMaxParticles];
+    int32_t big_list[kNoAllocMaxParticles / kBigVoxel + 1];
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// device address of g_noalloc_scratch per device ordinal, looked up once
+std::mutex g_noalloc_mutex;
+constexpr int kNoAllocMaxDevices = 64;
+NoAllocScratch* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(NoAllocScratch** out) {
+    int dev = 0;
+    SPHGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(SPHGB_ERR_RANGE, "device ordinal beyond the no-alloc table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_addr[dev] = static_cast<NoAllocScratch*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return SPHGB_OK;
+}
+
+}  // namespace
+
+extern "C" int sphgb_organize_voxels_noalloc(const SphgbSceneParams* scene, const float* d_pos,
+                                             const float* d_vel, const int32_t* d_pid,
+                                             float* d_pos_out, float* d_vel_out,
+                                             int32_t* d_pid_out, int32_t* d_voxel_start,
+                                             int32_t* d_voxel_count, void* stream) {
+    if (!scene) return fail(SPHGB_ERR_INVALID, "scene is null");
+    if (scene->particle_count > kNoAllocMaxParticles)
+        return fail(SPHGB_ERR_RANGE, "particle_count " + std::to_string(scene->particle_count) +
+                                         " exceeds the no-alloc limit of " +
+                                         std::to_string(kNoAllocMaxParticles));
+    SceneDev d;
+    // pipe rows are not used by this stage: accept the scene's own range
+    int rc = build_scene(*scene, (int)(scene->pipe_row_offset + scene->pipe_rows), d);
+    if (rc) return rc;
+    if ((int64_t)d.v_count + 1 > kNoAllocMaxVoxels)
+        return fail(SPHGB_ERR_RANGE, "voxel table of " + std::to_string((int64_t)d.v_count + 1) +
+                                         " entries exceeds the no-alloc limit of " +
+                                         std::to_string(kNoAllocMaxVoxels));
+    const int n = (int)scene->particle_count;
+    if (n > 0 && (!d_pos || !d_vel || !d_pid || !d_pos_out || !d_vel_out || !d_pid_out))
+        return fail(SPHGB_ERR_INVALID, "null buffer");
+    if (!d_voxel_start || !d_voxel_count) return fail(SPHGB_ERR_INVALID, "null voxel table");
+    NoAllocScratch* S = nullptr;
+    rc = noalloc_scratch(&S);
+    if (rc) return rc;
+    d.p_begin = 0;
+    d.p_count = n;
+    d.v_begin = 0;
+    const int32_t pbegin[2] = {0, n};
+    cudaStream_t st = as_stream(stream);
+    // the scene descriptor and the counters live in the shared array too: a
+    // later call overwrites them, so calls that overlap on the GPU race
+    SPHGB_CUDA(cudaMemcpyAsync(&S->scene, &d, sizeof(SceneDev), cudaMemcpyHostToDevice, st));
+    SPHGB_CUDA(cudaMemcpyAsync(S->pbegin, pbegin, sizeof(pbegin), cudaMemcpyHostToDevice, st));
+    SPHGB_CUDA(cudaMemsetAsync(S->counters, 0, sizeof(S->counters), st));
+    const int v_total = d.v_count + 1;
+    SPHGB_CUDA(cudaMemsetAsync(d_voxel_count, 0, sizeof(int32_t) * v_total, st));
+    if (n == 0) {
+        SPHGB_CUDA(cudaMemsetAsync(d_voxel_start, 0, sizeof(int32_t) * v_total, st));
+        return SPHGB_OK;
+    }
+    Launch L;
+    L.scenes = &S->scene;
+    L.pbegin = S->pbegin;
+    L.n_scenes = 1;
+    L.n = n;
+    L.v_total = v_total;
+    L.pipe = nullptr;
+    L.pipe_scenes = false;
+    L.stream = st;
+    const float4* pos = reinterpret_cast<const float4*>(d_pos);
+    SPHGB_CUDA(launch_hash_count(L, pos, S->cell, S->slot, d_voxel_count));
+    SPHGB_CUDA(launch_scan(L, d_voxel_count, d_voxel_start, S->tile_sums, scan_tiles(v_total)));
+    SPHGB_CUDA(launch_scatter(L, S->cell, S->slot, d_pid, d_voxel_start, d_voxel_count, S->tmp_pid,
+                              S->big_list, &S->counters[0]));
+    SPHGB_CUDA(launch_sort_big(L, S->big_list, &S->counters[0], d_voxel_start, d_voxel_count,
+                               S->tmp_pid));
+    SPHGB_CUDA(launch_rank_gather(L, S->cell, d_pid, S->tmp_pid, d_voxel_start, d_voxel_count, pos,
+                                  reinterpret_cast<const float4*>(d_vel), nullptr,
+                                  reinterpret_cast<float4*>(d_pos_out),
+                                  reinterpret_cast<float4*>(d_vel_out), d_pid_out, nullptr));
+    return SPHGB_OK;
+}

@@ -74,6 +74,7 @@ SIGNATURES = [
     ("sphgb_ctx_neighbour_counts", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_assign_voxels", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_organize_voxels", _I, [_VP] + [_VP] * 10 + [_VP]),
+    ("sphgb_organize_voxels_noalloc", _I, [C.POINTER(SceneParams)] + [_VP] * 9),
     ("sphgb_neighbours", _I, [_VP, _VP, _VP, _VP, _VP, _I, _VP, _VP, _VP]),
     ("sphgb_density", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     ("sphgb_forces", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),

@@ -178,6 +178,24 @@ int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
                           double* d_pos64_out, int32_t* d_voxel_start,
                           int32_t* d_voxel_count, void* stream);
 
+/* The voxel organisation of sphgb_organize_voxels without any device
+ * allocation, for callers that may not call cudaMalloc (their process forbids
+ * it, or all device memory goes through an allocator of their own).  No
+ * counterpart in the reference.  No context: the scene is passed directly
+ * (one scene; pipe rows are not needed).  Scratch lives in one file-scope
+ * __device__ array of fixed size (about 3.2 MB, held by every GPU that loads
+ * the library until exit); limits: particle_count <= 262,144 and
+ * ceil(space/voxel) voxels + 1 <= 4,194,304, else SPHGB_ERR_RANGE.  The first
+ * call on a device looks the array up (cudaGetSymbolAddress) with that device
+ * current; make it before any stream capture.  Every call shares the array and
+ * it keeps the last call's contents: calls that overlap on the GPU (other
+ * streams, other threads) race.  Outputs as sphgb_organize_voxels; the voxel
+ * table has ceil dims + 1 entries. */
+int sphgb_organize_voxels_noalloc(const SphgbSceneParams* scene, const float* d_pos,
+                                  const float* d_vel, const int32_t* d_pid, float* d_pos_out,
+                                  float* d_vel_out, int32_t* d_pid_out, int32_t* d_voxel_start,
+                                  int32_t* d_voxel_count, void* stream);
+
 /* get_neighbours (voxel_kernels.py:30-85) for every sorted slot: the ordered,
  * capped neighbour list (sorted slots, -1 padded; d_list may be NULL) with
  * list_stride entries per particle, and the capped/uncapped counts. */
