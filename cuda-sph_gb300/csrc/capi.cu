@@ -103,6 +103,17 @@ struct SphgbCtx {
     int n_chunks = 0;
     ConsChunk* d_chunks = nullptr;
     double* d_partials = nullptr;
+    // buffer capacities (elements), so reconfiguration reuses what is big enough
+    struct {
+        size_t scenes = 0, pbegin = 0, pipe = 0, cell = 0, slot = 0, tmp_pid = 0, vstart = 0,
+               vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, aux = 0, big_list = 0,
+               big_count = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
+               partials = 0;
+    } cap;
+    // tuning (sphgb_ctx_set_tuning)
+    int sort_block = 256;
+    int density_variant = SPHGB_DENSITY_WARP;
+    int big_voxel = kBigVoxel;
     // streams and graphs
     cudaStream_t cap_stream = nullptr;
     cudaStream_t host_stream = nullptr;
@@ -117,6 +128,8 @@ struct SphgbCtx {
         L.v_total = v_total;
         L.pipe = d_pipe;
         L.pipe_scenes = any_pipe;
+        L.sort_block = sort_block;
+        L.big_voxel = big_voxel;
         L.stream = st;
         return L;
     }
@@ -240,10 +253,11 @@ __global__ void k_load_aos(const SceneDev* __restrict__ scenes, const int32_t* _
     vel_out[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
     pid_out[i] = i - __ldg(pbegin + si);
     if (pos64_out) {
-        // the accumulator starts from the FP32 state, as the device state does
-        pos64_out[3 * i] = (double)(float)x;
-        pos64_out[3 * i + 1] = (double)(float)y;
-        pos64_out[3 * i + 2] = (double)(float)z;
+        // the FP64 accumulator takes the input as given (an exported pipe state
+        // reloads bit-exactly); FP32-representable input makes it equal pos
+        pos64_out[3 * i] = x;
+        pos64_out[3 * i + 1] = y;
+        pos64_out[3 * i + 2] = z;
     }
     (void)scenes;
 }
@@ -443,8 +457,11 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
                               p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
     if (rc) return rc;
-    SPHGB_CUDA(launch_density_wc(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
-                                 c->tasks, c->big_count + 1));
+    if (c->density_variant == SPHGB_DENSITY_WARP)
+        SPHGB_CUDA(launch_density_wc(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
+                                     c->tasks, c->big_count + 1));
+    else
+        SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
     const bool sep = c->out_pos != nullptr;
     SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB, p64B, c->vstart,
@@ -456,6 +473,119 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
     SPHGB_CUDA(cudaGetLastError());
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[7], st));
+    return SPHGB_OK;
+}
+
+// (Re)build the scene tables of a context and make every buffer large enough
+// for them; buffers keep their capacity and are only replaced when too small.
+template <class T>
+int ensure(T** p, size_t& cap, size_t need) {
+    if (need == 0) need = 1;
+    if (*p && cap >= need) return SPHGB_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cap = 0;
+    const size_t want = need + need / 4;   // grow with headroom
+    int rc = dalloc(p, want);
+    if (rc == SPHGB_OK) cap = want;
+    return rc;
+}
+
+int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
+              const double* pipe_rows_table, int n_pipe_rows_total) {
+    if (!scenes || n_scenes <= 0) return fail(SPHGB_ERR_INVALID, "need at least one scene");
+    if (n_pipe_rows_total < 0 || (n_pipe_rows_total > 0 && !pipe_rows_table))
+        return fail(SPHGB_ERR_INVALID, "bad pipe table");
+    std::vector<SceneDev> hs((size_t)n_scenes);
+    std::vector<int32_t> hp((size_t)n_scenes + 1);
+    int64_t n_tot = 0, v_tot = 0;
+    bool any_pipe = false;
+    for (int i = 0; i < n_scenes; ++i) {
+        int rc = build_scene(scenes[i], n_pipe_rows_total, hs[i]);
+        if (rc) return fail(rc, "scene " + std::to_string(i) + ": " + g_last_error);
+        SceneDev& d = hs[i];
+        d.p_begin = (int32_t)n_tot;
+        d.p_count = (int32_t)scenes[i].particle_count;
+        d.v_begin = (int32_t)v_tot;
+        hp[i] = (int32_t)n_tot;
+        n_tot += scenes[i].particle_count;
+        v_tot += d.v_count + 1;   // + the scene's overflow bucket
+        if (n_tot > (int64_t)0x7fffffff - 1 || v_tot > (int64_t)0x7fffffff - 1)
+            return fail(SPHGB_ERR_RANGE, "particles or voxels over 2^31 in one context");
+        if (d.mode == SPHGB_MODE_PIPE) any_pipe = true;
+    }
+    hp[n_scenes] = (int32_t)n_tot;
+    std::vector<ConsChunk> chunks;
+    for (int i = 0; i < n_scenes; ++i) {
+        const SceneDev& d = hs[i];
+        for (int b = 0; b < d.p_count; b += kConsChunk)
+            chunks.push_back({i, d.p_begin + b, d.p_begin + std::min(d.p_count, b + kConsChunk), 0});
+    }
+    const size_t N = (size_t)n_tot, V = (size_t)v_tot;
+    const int n_tiles = scan_tiles((int)v_tot);
+    auto& k = c->cap;
+    int rc = SPHGB_OK;
+    rc = rc ? rc : ensure(&c->d_scenes, k.scenes, (size_t)n_scenes);
+    rc = rc ? rc : ensure(&c->d_pbegin, k.pbegin, (size_t)n_scenes + 1);
+    rc = rc ? rc : ensure(&c->d_pipe, k.pipe, (size_t)n_pipe_rows_total * 5);
+    rc = rc ? rc : ensure(&c->cell, k.cell, N);
+    rc = rc ? rc : ensure(&c->slot, k.slot, N);
+    rc = rc ? rc : ensure(&c->tmp_pid, k.tmp_pid, N);
+    rc = rc ? rc : ensure(&c->vstart, k.vstart, V);
+    rc = rc ? rc : ensure(&c->vcount, k.vcount, V);
+    rc = rc ? rc : ensure(&c->tile_sums, k.tile_sums, (size_t)n_tiles);
+    rc = rc ? rc : ensure(&c->posB, k.posB, N);
+    rc = rc ? rc : ensure(&c->velB, k.velB, N);
+    rc = rc ? rc : ensure(&c->pidB, k.pidB, N);
+    rc = rc ? rc : ensure(&c->aux, k.aux, N);
+    rc = rc ? rc : ensure(&c->big_list, k.big_list, N / kMinBigVoxel + 1);
+    rc = rc ? rc : ensure(&c->big_count, k.big_count, 2);
+    rc = rc ? rc : ensure(&c->tasks, k.tasks, N);
+    rc = rc ? rc : ensure(&c->nbr.idx, k.nbr_idx, (size_t)kListCap * N);
+    rc = rc ? rc : ensure(&c->nbr.count, k.nbr_count, N);
+    if (any_pipe) rc = rc ? rc : ensure(&c->pos64B, k.pos64B, 3 * N);
+    rc = rc ? rc : ensure(&c->d_chunks, k.chunks, chunks.size());
+    rc = rc ? rc : ensure(&c->d_partials, k.partials, chunks.size() * 6);
+    if (rc) return rc;
+    SPHGB_CUDA(cudaMemcpy(c->d_scenes, hs.data(), sizeof(SceneDev) * n_scenes,
+                          cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->d_pbegin, hp.data(), sizeof(int32_t) * (n_scenes + 1),
+                          cudaMemcpyHostToDevice));
+    if (n_pipe_rows_total > 0)
+        SPHGB_CUDA(cudaMemcpy(c->d_pipe, pipe_rows_table, sizeof(double) * 5 * n_pipe_rows_total,
+                              cudaMemcpyHostToDevice));
+    if (!chunks.empty())
+        SPHGB_CUDA(cudaMemcpy(c->d_chunks, chunks.data(), sizeof(ConsChunk) * chunks.size(),
+                              cudaMemcpyHostToDevice));
+    c->h_scenes.swap(hs);
+    c->h_pbegin.swap(hp);
+    c->n_scenes = n_scenes;
+    c->n = (int)n_tot;
+    c->v_total = (int)v_tot;
+    c->n_tiles = n_tiles;
+    c->n_pipe_rows = n_pipe_rows_total;
+    c->n_chunks = (int)chunks.size();
+    c->any_pipe = any_pipe;
+    // the caller binds (new) state and outputs for the new layout
+    c->bound = false;
+    c->posA = c->velA = nullptr;
+    c->rho = nullptr;
+    c->pidA = nullptr;
+    c->pos64A = nullptr;
+    c->scene_step = nullptr;
+    c->out_pos = c->out_vel = nullptr;
+    c->out_pid = nullptr;
+    c->out_pos64 = nullptr;
+    if (c->owned) {
+        cudaFree(c->owned);
+        c->owned = nullptr;
+    }
+    if (c->stage) {
+        cudaFree(c->stage);
+        c->stage = nullptr;
+    }
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
     return SPHGB_OK;
 }
 
@@ -473,94 +603,54 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
                      int n_pipe_rows_total, SphgbCtx** out_ctx) {
     if (!out_ctx) return fail(SPHGB_ERR_INVALID, "out_ctx is null");
     *out_ctx = nullptr;
+    // argument checks before any CUDA call
     if (!scenes || n_scenes <= 0) return fail(SPHGB_ERR_INVALID, "need at least one scene");
     if (n_pipe_rows_total < 0 || (n_pipe_rows_total > 0 && !pipe_rows_table))
         return fail(SPHGB_ERR_INVALID, "bad pipe table");
+    for (int i = 0; i < n_scenes; ++i) {
+        SceneDev probe;
+        int rc = build_scene(scenes[i], n_pipe_rows_total, probe);
+        if (rc) return fail(rc, "scene " + std::to_string(i) + ": " + g_last_error);
+    }
     SphgbCtx* c = new (std::nothrow) SphgbCtx();
     if (!c) return fail(SPHGB_ERR_NOMEM, "host allocation failed");
     cudaGetDevice(&c->device);
-    c->n_scenes = n_scenes;
-    c->h_scenes.resize(n_scenes);
-    c->h_pbegin.resize(n_scenes + 1);
-    int64_t n_tot = 0, v_tot = 0;
-    for (int i = 0; i < n_scenes; ++i) {
-        int rc = build_scene(scenes[i], n_pipe_rows_total, c->h_scenes[i]);
-        if (rc) {
-            free_ctx(c);
-            return fail(rc, "scene " + std::to_string(i) + ": " + g_last_error);
-        }
-        SceneDev& d = c->h_scenes[i];
-        d.p_begin = (int32_t)n_tot;
-        d.p_count = (int32_t)scenes[i].particle_count;
-        d.v_begin = (int32_t)v_tot;
-        c->h_pbegin[i] = (int32_t)n_tot;
-        n_tot += scenes[i].particle_count;
-        v_tot += d.v_count + 1;   // + the scene's overflow bucket
-        if (n_tot > (int64_t)0x7fffffff - 1 || v_tot > (int64_t)0x7fffffff - 1) {
-            free_ctx(c);
-            return fail(SPHGB_ERR_RANGE, "particles or voxels over 2^31 in one context");
-        }
-        if (d.mode == SPHGB_MODE_PIPE) c->any_pipe = true;
-    }
-    c->h_pbegin[n_scenes] = (int32_t)n_tot;
-    c->n = (int)n_tot;
-    c->v_total = (int)v_tot;
-    c->n_tiles = scan_tiles(c->v_total);
-    c->n_pipe_rows = n_pipe_rows_total;
-    // conservation chunks
-    std::vector<ConsChunk> chunks;
-    for (int i = 0; i < n_scenes; ++i) {
-        const SceneDev& d = c->h_scenes[i];
-        for (int b = 0; b < d.p_count; b += kConsChunk)
-            chunks.push_back({i, d.p_begin + b, d.p_begin + std::min(d.p_count, b + kConsChunk), 0});
-    }
-    c->n_chunks = (int)chunks.size();
-    const size_t N = (size_t)c->n, V = (size_t)c->v_total;
-    int rc = SPHGB_OK;
-    rc = rc ? rc : dalloc(&c->d_scenes, (size_t)n_scenes);
-    rc = rc ? rc : dalloc(&c->d_pbegin, (size_t)n_scenes + 1);
-    rc = rc ? rc : dalloc(&c->d_pipe, (size_t)n_pipe_rows_total * 5);
-    rc = rc ? rc : dalloc(&c->cell, N);
-    rc = rc ? rc : dalloc(&c->slot, N);
-    rc = rc ? rc : dalloc(&c->tmp_pid, N);
-    rc = rc ? rc : dalloc(&c->vstart, V);
-    rc = rc ? rc : dalloc(&c->vcount, V);
-    rc = rc ? rc : dalloc(&c->tile_sums, (size_t)c->n_tiles);
-    rc = rc ? rc : dalloc(&c->posB, N);
-    rc = rc ? rc : dalloc(&c->velB, N);
-    rc = rc ? rc : dalloc(&c->pidB, N);
-    rc = rc ? rc : dalloc(&c->aux, N);
-    rc = rc ? rc : dalloc(&c->big_list, N / kBigVoxel + 1);
-    rc = rc ? rc : dalloc(&c->big_count, 2);
-    rc = rc ? rc : dalloc(&c->tasks, N);
-    rc = rc ? rc : dalloc(&c->nbr.idx, (size_t)kListCap * N);
-    rc = rc ? rc : dalloc(&c->nbr.count, N);
-    if (c->any_pipe) rc = rc ? rc : dalloc(&c->pos64B, 3 * N);
-    rc = rc ? rc : dalloc(&c->d_chunks, chunks.size());
-    rc = rc ? rc : dalloc(&c->d_partials, chunks.size() * 6);
-    if (rc) {
-        std::string m = g_last_error;
-        free_ctx(c);
-        return fail(rc, m);
-    }
-    cudaError_t e = cudaMemcpy(c->d_scenes, c->h_scenes.data(), sizeof(SceneDev) * n_scenes,
-                               cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(c->d_pbegin, c->h_pbegin.data(), sizeof(int32_t) * (n_scenes + 1),
-                       cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && n_pipe_rows_total > 0)
-        e = cudaMemcpy(c->d_pipe, pipe_rows_table, sizeof(double) * 5 * n_pipe_rows_total,
-                       cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !chunks.empty())
-        e = cudaMemcpy(c->d_chunks, chunks.data(), sizeof(ConsChunk) * chunks.size(),
-                       cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         free_ctx(c);
         return cuda_fail(e, "sphgb_ctx_create");
     }
+    int rc = configure(c, scenes, n_scenes, pipe_rows_table, n_pipe_rows_total);
+    if (rc) {
+        std::string m = g_last_error;
+        free_ctx(c);
+        return fail(rc, m);
+    }
     *out_ctx = c;
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_reconfigure(SphgbCtx* ctx, const SphgbSceneParams* scenes, int n_scenes,
+                          const double* pipe_rows_table, int n_pipe_rows_total) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    SPHGB_CUDA(cudaDeviceSynchronize());   // nothing in flight may use the old tables
+    return configure(ctx, scenes, n_scenes, pipe_rows_table, n_pipe_rows_total);
+}
+
+int sphgb_ctx_set_tuning(SphgbCtx* ctx, int sort_block, int density_variant, int big_voxel) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (sort_block != 128 && sort_block != 256 && sort_block != 512)
+        return fail(SPHGB_ERR_INVALID, "sort_block must be 128, 256 or 512");
+    if (density_variant != SPHGB_DENSITY_WARP && density_variant != SPHGB_DENSITY_THREAD)
+        return fail(SPHGB_ERR_INVALID, "density_variant must be SPHGB_DENSITY_WARP or _THREAD");
+    if (big_voxel < kMinBigVoxel || big_voxel > 4096)
+        return fail(SPHGB_ERR_INVALID, "big_voxel must be in [16, 4096]");
+    ctx->sort_block = sort_block;
+    ctx->density_variant = density_variant;
+    ctx->big_voxel = big_voxel;
+    for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
     return SPHGB_OK;
 }
 

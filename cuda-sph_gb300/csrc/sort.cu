@@ -58,7 +58,7 @@ __device__ __forceinline__ int block_excl_scan(int v, int& total) {
     return incl - v + warp_off[wid];
 }
 
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(512)
 k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
              int n, const float4* __restrict__ pos, int32_t* __restrict__ cell,
              int32_t* __restrict__ slot, int32_t* __restrict__ vcount) {
@@ -160,17 +160,17 @@ k_tile_scan(const int32_t* __restrict__ vcount, int v_total, const int32_t* __re
     }
 }
 
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(512)
 k_scatter(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ slot,
           const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
           const int32_t* __restrict__ vcount, int32_t* __restrict__ tmp_pid,
-          int32_t* __restrict__ big_list, int32_t* __restrict__ big_count) {
+          int32_t* __restrict__ big_list, int32_t* __restrict__ big_count, int big_voxel) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int vid = cell[s];
     const int sl = slot[s];
     tmp_pid[__ldg(vstart + vid) + sl] = pid[s];
-    if (sl == 0 && __ldg(vcount + vid) > kBigVoxel) big_list[atomicAdd(big_count, 1)] = vid;
+    if (sl == 0 && __ldg(vcount + vid) > big_voxel) big_list[atomicAdd(big_count, 1)] = vid;
 }
 
 // One block per big voxel (grid-stride over the list): sorts the voxel's
@@ -227,14 +227,14 @@ k_sort_big(const int32_t* __restrict__ big_list, const int32_t* __restrict__ big
     }
 }
 
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(512)
 k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ pid,
               const int32_t* __restrict__ tmp_pid, const int32_t* __restrict__ vstart,
               const int32_t* __restrict__ vcount, const float4* __restrict__ pos,
               const float4* __restrict__ vel, const double* __restrict__ pos64,
               float4* __restrict__ pos_out, float4* __restrict__ vel_out,
               int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
-              int2* __restrict__ tasks, int32_t* __restrict__ task_count) {
+              int2* __restrict__ tasks, int32_t* __restrict__ task_count, int big_voxel) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int vid = cell[s];
@@ -242,7 +242,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
     const int st = __ldg(vstart + vid);
     const int c = __ldg(vcount + vid);
     int r = 0;
-    if (c <= kBigVoxel) {
+    if (c <= big_voxel) {
         for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
     } else {                            // sorted by k_sort_big: lower bound of p
         int lo = 0, hi = c;
@@ -273,8 +273,9 @@ int scan_tiles(int v_total) { return (v_total + kScanTile - 1) / kScanTile; }
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
                               int32_t* vcount) {
     if (L.n == 0) return cudaSuccess;
-    k_hash_count<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n,
-                                                            pos, cell, slot, vcount);
+    const int b = L.sort_block;
+    k_hash_count<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
+                                                        cell, slot, vcount);
     return cudaGetLastError();
 }
 
@@ -291,8 +292,9 @@ cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* 
                            const int32_t* pid, const int32_t* vstart, const int32_t* vcount,
                            int32_t* tmp_pid, int32_t* big_list, int32_t* big_count) {
     if (L.n == 0) return cudaSuccess;
-    k_scatter<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, slot, pid, vstart, vcount,
-                                                         tmp_pid, big_list, big_count);
+    const int b = L.sort_block;
+    k_scatter<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.n, cell, slot, pid, vstart, vcount, tmp_pid,
+                                                     big_list, big_count, L.big_voxel);
     return cudaGetLastError();
 }
 
@@ -311,10 +313,11 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
                                int32_t* pid_out, double* pos64_out, int2* tasks,
                                int32_t* task_count) {
     if (L.n == 0) return cudaSuccess;
-    k_rank_gather<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart,
-                                                             vcount, pos, vel, pos64, pos_out,
-                                                             vel_out, pid_out, pos64_out, tasks,
-                                                             task_count);
+    const int b = L.sort_block;
+    k_rank_gather<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart, vcount,
+                                                         pos, vel, pos64, pos_out, vel_out,
+                                                         pid_out, pos64_out, tasks, task_count,
+                                                         L.big_voxel);
     return cudaGetLastError();
 }
 

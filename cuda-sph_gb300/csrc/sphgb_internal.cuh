@@ -368,6 +368,8 @@ struct Launch {
     int v_total;                // voxels (all scenes)
     const double* pipe;         // device pipe table (may be null)
     bool pipe_scenes;           // some scene is in pipe mode
+    int sort_block = kBlock;    // threads per block of the per-particle sort kernels
+    int big_voxel = 64;         // voxels above this many members are sorted per block
     cudaStream_t stream;
 };
 
@@ -379,9 +381,11 @@ int scan_tiles(int v_total);
 cudaError_t launch_scatter(const Launch& L, const int32_t* cell, const int32_t* slot,
                            const int32_t* pid, const int32_t* vstart, const int32_t* vcount,
                            int32_t* tmp_pid, int32_t* big_list, int32_t* big_count);
-// voxels with more than kBigVoxel members get their member ids sorted by one
-// block each (the rank-gather then binary-searches them instead of counting)
+// voxels with more than Launch::big_voxel members (default kBigVoxel) get their
+// member ids sorted by one block each (the rank-gather then binary-searches
+// them instead of counting); the threshold is never below kMinBigVoxel
 constexpr int kBigVoxel = 64;
+constexpr int kMinBigVoxel = 16;
 cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
 // tasks (optional): one (voxel, first slot) entry per run of up to 32 sorted

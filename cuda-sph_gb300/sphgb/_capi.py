@@ -13,6 +13,7 @@ from . import _build
 
 MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
+DENSITY_WARP, DENSITY_THREAD = 0, 1
 
 ERRORS = {
     -1: "SPHGB_ERR_INVALID",
@@ -62,6 +63,8 @@ SIGNATURES = [
     ("sphgb_last_error", C.c_char_p, []),
     ("sphgb_ctx_create", _I, [C.POINTER(SceneParams), _I, _VP, _I, C.POINTER(_VP)]),
     ("sphgb_ctx_destroy", _I, [_VP]),
+    ("sphgb_ctx_reconfigure", _I, [_VP, C.POINTER(SceneParams), _I, _VP, _I]),
+    ("sphgb_ctx_set_tuning", _I, [_VP, _I, _I, _I]),
     ("sphgb_ctx_sizes", _I, [_VP, C.POINTER(_I64), C.POINTER(_I64)]),
     ("sphgb_ctx_bind_state", _I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     ("sphgb_ctx_bind_output", _I, [_VP, _VP, _VP, _VP, _VP]),

@@ -70,26 +70,40 @@ class SceneBatch:
     def __init__(self, specs: Sequence[SceneSpec], device: str = "cuda"):
         import torch
         self._torch = torch
-        self.specs: List[SceneSpec] = list(specs)
-        if not self.specs:
-            raise ValueError("need at least one scene")
         self.device = torch.device(device)
-        lib = _capi.load()
+        self._ctx = None
+        self.out_pos = self.out_vel = self.out_pid = self.out_pos64 = None
+        self._configure(specs)
+
+    def _tables(self, specs):
         rows, params = [], []
-        for s in self.specs:
+        for s in specs:
             params.append(scene_params(s, pipe_row_offset=len(rows)))
             if s.mode == 'PIPE':
                 rows.extend(np.asarray(s.params.pipe.to_numpy(), dtype=np.float64))
-        self.pipe_table = (np.ascontiguousarray(np.stack(rows), dtype=np.float64)
-                           if rows else np.zeros((0, 5)))
-        arr = (_capi.SceneParams * len(params))(*params)
-        self._params = arr
-        handle = C.c_void_p()
+        table = (np.ascontiguousarray(np.stack(rows), dtype=np.float64) if rows
+                 else np.zeros((0, 5)))
+        return (_capi.SceneParams * len(params))(*params), table, len(rows)
+
+    def _configure(self, specs, steps=None):
+        torch = self._torch
+        specs = list(specs)
+        if not specs:
+            raise ValueError("need at least one scene")
+        lib = _capi.load()
+        arr, table, n_rows = self._tables(specs)
+        pipe_ptr = table.ctypes.data if n_rows else None
         with torch.cuda.device(self.device):
-            _capi.check(lib.sphgb_ctx_create(arr, len(params),
-                                             self.pipe_table.ctypes.data if rows else None,
-                                             len(rows), C.byref(handle)), "sphgb_ctx_create")
-        self._ctx = handle
+            if self._ctx is None:
+                handle = C.c_void_p()
+                _capi.check(lib.sphgb_ctx_create(arr, len(specs), pipe_ptr, n_rows,
+                                                 C.byref(handle)), "sphgb_ctx_create")
+                self._ctx = handle
+            else:
+                _capi.check(lib.sphgb_ctx_reconfigure(self._ctx, arr, len(specs), pipe_ptr, n_rows),
+                            "sphgb_ctx_reconfigure")
+        self.specs = specs
+        self._params, self.pipe_table = arr, table
         n = C.c_int64()
         v = C.c_int64()
         _capi.check(lib.sphgb_ctx_sizes(self._ctx, C.byref(n), C.byref(v)), "sphgb_ctx_sizes")
@@ -104,11 +118,25 @@ class SceneBatch:
         self.pid = torch.zeros((max(self.n, 1),), dtype=torch.int32, device=dev)
         self.pos64 = torch.zeros((max(self.n, 1) if self.any_pipe else 1, 3),
                                  dtype=torch.float64, device=dev)
-        self.steps = torch.zeros((len(self.specs),), dtype=torch.int32, device=dev)
+        self.steps = (torch.zeros((len(self.specs),), dtype=torch.int32, device=dev)
+                      if steps is None else steps.to(dev, torch.int32).contiguous())
         _capi.check(lib.sphgb_ctx_bind_state(
             self._ctx, self.pos.data_ptr(), self.vel.data_ptr(), self.rho.data_ptr(),
             self.pid.data_ptr(), self.pos64.data_ptr(), self.steps.data_ptr()),
             "sphgb_ctx_bind_state")
+        self.out_pos = self.out_vel = self.out_pid = self.out_pos64 = None
+
+    def reconfigure(self, specs: Sequence[SceneSpec], steps=None) -> None:
+        """Replace the scenes, reusing the context's scratch where it fits.
+        The state is reset (load new states afterwards); ``steps`` optionally
+        gives each scene's step count (the respawn stream position)."""
+        self._configure(specs, steps)
+
+    def set_tuning(self, sort_block: int = 256, density_variant: int = _capi.DENSITY_WARP,
+                   big_voxel: int = 64) -> None:
+        """Launch tuning; results are unchanged (see sphgb_ctx_set_tuning)."""
+        _capi.call("sphgb_ctx_set_tuning", self._ctx, int(sort_block), int(density_variant),
+                   int(big_voxel))
 
     # -- helpers ---------------------------------------------------------
     def _stream(self, stream=None) -> int:
@@ -165,11 +193,12 @@ class SceneBatch:
         self.load_aos_device(torch.from_numpy(np.ascontiguousarray(pos)).to(self.device),
                              torch.from_numpy(np.ascontiguousarray(vel)).to(self.device), stream)
 
-    def load_aos_device(self, pos_aos, vel_aos, stream=None) -> None:
+    def load_aos_device(self, pos_aos, vel_aos, stream=None, reset_steps=True) -> None:
         """Load FP64 (N, 3) device tensors in original order (scene-concatenated)."""
         _capi.call("sphgb_ctx_load_aos_f64", self._ctx, pos_aos.data_ptr(), vel_aos.data_ptr(),
                    self._stream(stream))
-        self.steps.zero_()
+        if reset_steps:
+            self.steps.zero_()
 
     def export_aos_f64(self, stream=None):
         """(pos, vel, rho) as FP64 device tensors in original particle order."""

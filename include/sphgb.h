@@ -44,6 +44,7 @@ enum {
 
 enum { SPHGB_MODE_BOX = 0, SPHGB_MODE_PIPE = 1 };      /* config.SIM_MODE (config.py:13) */
 enum { SPHGB_WALK_CEIL = 0, SPHGB_WALK_TRUNCATED = 1 }; /* see walk_dims below */
+enum { SPHGB_DENSITY_WARP = 0, SPHGB_DENSITY_THREAD = 1 }; /* sphgb_ctx_set_tuning */
 
 /*
  * One scene: SimulationParameters (common/data_classes.py:70-78) plus the
@@ -99,6 +100,20 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes,
                      const double* pipe_rows_table, int n_pipe_rows_total,
                      SphgbCtx** out_ctx);
 int sphgb_ctx_destroy(SphgbCtx* ctx);
+/* Replace the context's scenes (same arguments as sphgb_ctx_create), reusing
+ * every scratch buffer that is still large enough.  Synchronises the device.
+ * Bound state and outputs are unbound: bind state for the new layout before
+ * stepping.  Used by request servers whose scene set changes between batches;
+ * the reference creates one strategy per run instead (state_generator.py:21-23). */
+int sphgb_ctx_reconfigure(SphgbCtx* ctx, const SphgbSceneParams* scenes, int n_scenes,
+                          const double* pipe_rows_table, int n_pipe_rows_total);
+/* Launch tuning (results do not change): threads per block of the
+ * per-particle sort kernels (128, 256, 512), the density kernel variant
+ * (SPHGB_DENSITY_WARP: one warp per voxel run; SPHGB_DENSITY_THREAD: one
+ * thread per particle) and the member count above which a voxel is sorted by
+ * a block of its own (16..4096).  No counterpart in the reference (numba picks
+ * one block size per device, thread_layout.py:27-33). */
+int sphgb_ctx_set_tuning(SphgbCtx* ctx, int sort_block, int density_variant, int big_voxel);
 /* Total particles / voxel-table entries over all scenes of the context.  A
  * scene's table has ceil(space/voxel) voxels plus one overflow entry (last)
  * that collects particles with non-finite coordinates; no walk visits it. */
