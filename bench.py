@@ -70,6 +70,11 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=2, help="oracle steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched/served sections")
+    ap.add_argument("--batched-scenes", type=int, default=256)
+    ap.add_argument("--batched-steps", type=int, default=50)
+    ap.add_argument("--served-requests", type=int, default=24)
+    ap.add_argument("--served-rate", type=float, default=64.0, help="Poisson arrivals per second")
     return ap.parse_args()
 
 
@@ -321,12 +326,82 @@ def run_gb300(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(spec, state, args.cpu_steps)
         log(f"cpu baseline: {out['cpu_baseline']}")
+    batch.close()
+    if not args.no_batched and args.workload == "config2":
+        out["batched"] = batched_section(args)
+        out["served"] = served_section(args)
     if rank == 0:
         print(json.dumps(out), flush=True)
-    batch.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def batched_section(args):
+    """Batched scenes (256 boxes, N log-uniform in [1024, 65536], 50 steps):
+    one graph launch for all scenes against one scene per launch."""
+    import numpy as np
+    from oracle import ref
+    from sphgb import scenes
+    from sphgb.batch import particle_steps, run_batched, run_plain
+    pairs = scenes.config3_specs(n_scenes=args.batched_scenes, seed=3)
+    steps = args.batched_steps
+    work = particle_steps([p[0] for p in pairs], steps)
+    tb, sb = run_batched(pairs, steps, repeats=2)
+    log(f"batched: {len(pairs)} scenes, {work} particle-steps in {tb:.4f} s")
+    tp, sp_ = run_plain(pairs, steps)
+    log(f"plain (one scene per launch): {tp:.4f} s")
+    tg, _ = run_plain(pairs, steps, use_graph=True)
+    log(f"plain with one graph per scene: {tg:.4f} s")
+    same = all(np.array_equal(a.position, b.position) and np.array_equal(a.density, b.density)
+               for a, b in zip(sb, sp_))
+    # density error of the first step against the FP64 oracle, 8 scenes
+    _, one = run_batched(pairs[:8], 1, repeats=0)
+    err = 0.0
+    for (spec, st), got in zip(pairs[:8], one):
+        _, _, rho = ref.step(ref.params_from_spec(spec), st.position, st.velocity)
+        err = max(err, float(np.max(np.abs(got.density - rho) / rho)))
+    return {"scenes": len(pairs), "particles": sum(p[0].n for p in pairs), "steps": steps,
+            "value": work / tb, "unit": "particle-steps/s",
+            "plain_value": work / tp, "plain_graph_value": work / tg,
+            "vs_plain": tb and tp / tb, "vs_plain_graph": tg / tb,
+            "identical_to_plain": bool(same), "density_rel_err_vs_fp64": err,
+            "graph": "all scenes and steps in one CUDA graph launch"}
+
+
+def served_section(args):
+    """Served workload: Poisson arrivals, 70 % box / 30 % pipe, N log-uniform
+    in [2048, 524288], steps uniform in [100, 2000], 150 GB HBM budget;
+    continuous batching against serving the same requests one at a time."""
+    import numpy as np
+    from sphgb.device import SceneBatch
+    from sphgb.serve import SceneServer, poisson_requests
+    reqs = poisson_requests(args.served_rate, args.served_requests, seed=4)
+    work = sum(r.spec.n * r.steps for r in reqs)
+    server = SceneServer(hbm_budget_bytes=150e9, max_tick_steps=64)
+    st = server.run(reqs)
+    server.close()
+    log(f"served: {st.requests} requests, {work} particle-steps in {st.wall_s:.3f} s, "
+        f"p50 {st.pct(50):.3f} s p99 {st.pct(99):.3f} s, max active {st.max_active}")
+    import torch
+    plain_s = 0.0
+    for r in reqs:
+        b = SceneBatch([r.spec])
+        b.load_states([r.state])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.step(r.steps)
+        e1.record()
+        torch.cuda.synchronize()
+        plain_s += e0.elapsed_time(e1) / 1e3
+        b.close()
+    log(f"served one at a time: {plain_s:.3f} s of GPU time")
+    return {"requests": st.requests, "rate_per_s": args.served_rate, "value": st.throughput,
+            "unit": "particle-steps/s", "wall_s": st.wall_s, "p50_latency_s": st.pct(50),
+            "p99_latency_s": st.pct(99), "max_active": st.max_active, "ticks": st.ticks,
+            "repacks": st.repacks, "plain_value": work / plain_s,
+            "vs_plain": (work / st.wall_s) / (work / plain_s), "hbm_budget_gb": 150}
 
 
 def run_reference(args):

@@ -440,7 +440,7 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                               c->big_count));
     SPHGB_CUDA(launch_sort_big(L, c->big_list, c->big_count, vstart, vcount, c->tmp_pid));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[2], st));
-    SPHGB_CUDA(launch_rank_gather(L, c->cell, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
+    SPHGB_CUDA(launch_rank_gather(L, c->cell, c->slot, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
                                   pos_o, vel_o, pid_o, pos64_o, with_tasks ? c->tasks : nullptr,
                                   with_tasks ? c->big_count + 1 : nullptr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[3], st));
@@ -1143,7 +1143,7 @@ extern "C" int sphgb_organize_voxels_noalloc(const SphgbSceneParams* scene, cons
                               S->big_list, &S->counters[0]));
     SPHGB_CUDA(launch_sort_big(L, S->big_list, &S->counters[0], d_voxel_start, d_voxel_count,
                                S->tmp_pid));
-    SPHGB_CUDA(launch_rank_gather(L, S->cell, d_pid, S->tmp_pid, d_voxel_start, d_voxel_count, pos,
+    SPHGB_CUDA(launch_rank_gather(L, S->cell, S->slot, d_pid, S->tmp_pid, d_voxel_start, d_voxel_count, pos,
                                   reinterpret_cast<const float4*>(d_vel), nullptr,
                                   reinterpret_cast<float4*>(d_pos_out),
                                   reinterpret_cast<float4*>(d_vel_out), d_pid_out, nullptr));

@@ -75,7 +75,7 @@ k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
     } else {
         vid = sc.v_begin + sc.v_count;   // overflow bucket
     }
-    cell[s] = vid;
+    cell[s] = finite3(p) ? vid : ~vid;   // negative: overflow bucket (no pid order needed)
     slot[s] = atomicAdd(vcount + vid, 1);
 }
 
@@ -167,10 +167,13 @@ k_scatter(int n, const int32_t* __restrict__ cell, const int32_t* __restrict__ s
           int32_t* __restrict__ big_list, int32_t* __restrict__ big_count, int big_voxel) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const int vid = cell[s];
+    const int code = cell[s];
+    const int vid = code < 0 ? ~code : code;
     const int sl = slot[s];
     tmp_pid[__ldg(vstart + vid) + sl] = pid[s];
-    if (sl == 0 && __ldg(vcount + vid) > big_voxel) big_list[atomicAdd(big_count, 1)] = vid;
+    // overflow buckets (non-finite particles, never walked) keep arrival order
+    if (code >= 0 && sl == 0 && __ldg(vcount + vid) > big_voxel)
+        big_list[atomicAdd(big_count, 1)] = vid;
 }
 
 // One block per big voxel (grid-stride over the list): sorts the voxel's
@@ -234,15 +237,19 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
               const float4* __restrict__ vel, const double* __restrict__ pos64,
               float4* __restrict__ pos_out, float4* __restrict__ vel_out,
               int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
-              int2* __restrict__ tasks, int32_t* __restrict__ task_count, int big_voxel) {
+              int2* __restrict__ tasks, int32_t* __restrict__ task_count, int big_voxel,
+              const int32_t* __restrict__ slot) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const int vid = cell[s];
+    const int code = cell[s];
+    const int vid = code < 0 ? ~code : code;
     const int p = pid[s];
     const int st = __ldg(vstart + vid);
     const int c = __ldg(vcount + vid);
     int r = 0;
-    if (c <= big_voxel) {
+    if (code < 0) {
+        r = slot[s];                    // overflow bucket: arrival order, no pid order
+    } else if (c <= big_voxel) {
         for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
     } else {                            // sorted by k_sort_big: lower bound of p
         int lo = 0, hi = c;
@@ -306,8 +313,8 @@ cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int3
     return cudaGetLastError();
 }
 
-cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
-                               const int32_t* tmp_pid, const int32_t* vstart,
+cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* slot,
+                               const int32_t* pid, const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,
                                const double* pos64, float4* pos_out, float4* vel_out,
                                int32_t* pid_out, double* pos64_out, int2* tasks,
@@ -317,7 +324,7 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
     k_rank_gather<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart, vcount,
                                                          pos, vel, pos64, pos_out, vel_out,
                                                          pid_out, pos64_out, tasks, task_count,
-                                                         L.big_voxel);
+                                                         L.big_voxel, slot);
     return cudaGetLastError();
 }
 

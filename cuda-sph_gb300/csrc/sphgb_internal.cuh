@@ -373,6 +373,7 @@ struct Launch {
     cudaStream_t stream;
 };
 
+// cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow bucket
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
                               int32_t* vcount);
 cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
@@ -390,8 +391,8 @@ cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int3
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
 // tasks (optional): one (voxel, first slot) entry per run of up to 32 sorted
 // slots of a voxel, appended at task_count
-cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* pid,
-                               const int32_t* tmp_pid, const int32_t* vstart,
+cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* slot,
+                               const int32_t* pid, const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,
                                const double* pos64, float4* pos_out, float4* vel_out,
                                int32_t* pid_out, double* pos64_out, int2* tasks = nullptr,

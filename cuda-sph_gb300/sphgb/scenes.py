@@ -19,7 +19,10 @@ All positions, velocities and constants are FP32-representable.
   [0.5, 2], gravity 9.81 in a uniform direction, spacing min(0.02, 0.9 L/2nx),
   mass 1000 s^3, h 1.93 s (about 30 neighbours).
 * ``served_request``: one request of the served workload: 70 % box / 30 %
-  pipe, N log-uniform in [2048, 524288], steps uniform in [100, 2000].
+  pipe, N log-uniform in [2048, 524288], steps uniform in [100, 2000].  Box
+  requests are config 0 scaled to N (same spacing, h and mass; the box edge
+  grows to 1.25 x the block height), pipe requests config 1 scaled to N (h
+  scaled to keep its neighbour count).
 """
 from __future__ import annotations
 
@@ -122,10 +125,12 @@ def served_request(rng, n_min=2048, n_max=524_288, box_frac=0.7):
     steps = int(rng.integers(100, 2001))
     seed = int(rng.integers(1 << 31))
     if rng.uniform() < box_frac:
+        # config 0 scaled to N: its spacing, h and mass, the box grown to fit
+        # the block (the reference's formulas are stable there, unlike at the
+        # smaller h a fixed box would need)
         nx = max(2, int(round((n_target / 2.0) ** (1.0 / 3.0))))
-        s = min(0.02, 0.9 / (2 * nx))
-        spec, st = box_dam_break(nx=nx, ny=2 * nx, nz=nx, spacing=s, jitter=s / 10.0,
-                                 h=2.25 * s, mass=1000.0 * s ** 3, seed=seed)
+        edge = max(1.0, 1.25 * 2 * nx * 0.02)
+        spec, st = box_dam_break(nx=nx, ny=2 * nx, nz=nx, box=(edge, edge, edge), seed=seed)
     else:
         n = int(n_target)
         spec, st = pipe_flow(n=n, h=0.02 * (262_144 / n) ** (1.0 / 3.0), seed=seed)

@@ -180,11 +180,14 @@ int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_unca
 /* ---- stages (each launches the same kernels sphgb_ctx_step uses) ------- */
 
 /* assign_voxels_to_particles_kernel (voxel_kernels.py:89-105): voxel id of
- * each particle (ceil dims; coordinates clamped to the table). */
+ * each particle (ceil dims; coordinates clamped to the table).  A particle
+ * with a non-finite coordinate gets ~id (negative) of its scene's overflow
+ * entry, the last entry of the scene's voxel table. */
 int sphgb_assign_voxels(SphgbCtx* ctx, const float* d_pos, int32_t* d_voxel_out, void* stream);
 
 /* Voxel sort + voxel_begin (voxel_sph_strategy.py:65-107): stable counting
- * sort by (voxel id, particle id).  Reads state (d_pos, d_vel, d_pid) in any
+ * sort by (voxel id, particle id); particles of a scene's overflow entry
+ * (non-finite coordinates, never walked) come last, in arrival order.  Reads state (d_pos, d_vel, d_pid) in any
  * order, writes it voxel-sorted to the *_out buffers, and writes the voxel
  * table: d_voxel_start[v] (first sorted slot) and d_voxel_count[v]. */
 int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,

@@ -42,10 +42,10 @@ def test_clusters_and_nonfinite_sort_exactly():
     nv = len(rcount)
     # finite particles: exactly the oracle's order, and they fill the table first
     np.testing.assert_array_equal(ids[:finite.sum()], spid[finite[spid]])
-    # non-finite particles: the overflow bucket (last entry), ascending particle id
+    # non-finite particles: the overflow bucket (last entry), in arrival order
     assert count[nv] == (~finite).sum()
     over = ids[start[nv]:start[nv] + count[nv]]
-    np.testing.assert_array_equal(over, np.sort(np.nonzero(~finite)[0]))
+    np.testing.assert_array_equal(np.sort(over), np.nonzero(~finite)[0])
     assert count.max() >= 9000      # the cluster plus the voxel's own particles
     batch.close()
 
