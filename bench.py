@@ -229,7 +229,12 @@ def run_gb300(args):
     spec, state, desc = workload(args.workload)
     n = spec.n
     log(f"workload {args.workload}: {n} particles")
+    # launch tuning picked by the autotuner on this scene (results unchanged)
+    from sphgb.autotune import autotune, summary
+    best, tried = autotune([(spec, state)], steps=3, device=str(dev))
+    log(f"autotune: best {best}")
     batch = SceneBatch([spec], device=str(dev))
+    best.apply(batch)
     batch.load_states([state])
     # every timed step is a full compute_next_state of the same resident
     # input: the step writes to separate output buffers (see module docstring)
@@ -322,6 +327,9 @@ def run_gb300(args):
                       "input": "every step is a full step of the same resident step-0 state"},
            "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
            "free_running": free,
+           "autotune": {"chosen": {"density": "warp" if best.density_variant == 0 else "thread",
+                                   "sort_block": best.sort_block, "big_voxel": best.big_voxel},
+                        "ms_per_step": summary(tried)},
            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(spec, state, args.cpu_steps)
