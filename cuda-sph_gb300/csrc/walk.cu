@@ -90,6 +90,32 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
                 &s_list[0][threadIdx.x], kBlock);
 }
 
+// ---- packed FP32 pairs (PTX .f32x2; each half rounds like the scalar op) ----
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2pack(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2unpack(f32x2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2sub(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // Warp-cooperative density pass of the step.  One warp per task: up to 32
 // particles of one voxel (tasks listed by the rank-gather).  The 27 walk
 // voxels of that voxel are laid end to end in walk order; each batch of 32
@@ -105,6 +131,8 @@ constexpr int kWcList = kListCap;       // accepted neighbours per particle, sel
 
 struct WcShared {
     float4 home[32];
+    ulonglong2 home_xy[32];   // (x, x), (y, y) of each home particle, packed
+    f32x2 home_z[32];         // (z, z)
     int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
     int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
     int32_t st[27];     // first slot of each walk voxel
@@ -141,7 +169,11 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             __syncwarp();
             continue;
         }
-        if (home) S.home[lane] = pi;
+        if (home) {
+            S.home[lane] = pi;
+            S.home_xy[lane] = make_ulonglong2(f2pack(pi.x, pi.x), f2pack(pi.y, pi.y));
+            S.home_z[lane] = f2pack(pi.z, pi.z);
+        }
         // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
         int ck = 0, stk = 0;
         if (lane < 27) {
@@ -167,19 +199,33 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
         const double h_d = sc.h_d;
         int cnt = 0;    // lane i: accepted candidates of home particle i so far
-        for (int b0 = 0; b0 < M; b0 += 32) {
-            const int q = b0 + lane;
-            float4 pj = make_float4(0.f, 0.f, 0.f, 0.f);
-            int sj = -1;
-            if (q < M) {
+        // 64 candidates per batch, two per lane (q0 = b0 + lane, q1 = q0 + 32),
+        // their distances computed as packed FP32 pairs
+        for (int b0 = 0; b0 < M; b0 += 64) {
+            const int q0 = b0 + lane, q1 = q0 + 32;
+            const bool v0 = q0 < M, v1 = q1 < M;
+            float4 pj0 = make_float4(0.f, 0.f, 0.f, 0.f), pj1 = pj0;
+            int sj0 = -1, sj1 = -1;
+            if (v0) {
                 int lo = 0, hi = 26;            // last walk voxel with P <= q
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (S.P[mid] <= q) lo = mid; else hi = mid - 1;
+                    if (S.P[mid] <= q0) lo = mid; else hi = mid - 1;
                 }
-                sj = S.st[lo] + (q - S.P[lo]);
-                pj = __ldg(pos + sj);
+                sj0 = S.st[lo] + (q0 - S.P[lo]);
+                pj0 = __ldg(pos + sj0);
             }
+            if (v1) {
+                int lo = 0, hi = 26;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (S.P[mid] <= q1) lo = mid; else hi = mid - 1;
+                }
+                sj1 = S.st[lo] + (q1 - S.P[lo]);
+                pj1 = __ldg(pos + sj1);
+            }
+            const f32x2 cx = f2pack(pj0.x, pj1.x), cy = f2pack(pj0.y, pj1.y),
+                        cz = f2pack(pj0.z, pj1.z);
             // home particles still below the cap
             unsigned todo = __ballot_sync(full, home && cnt < cap);
             if (!todo) break;
@@ -187,21 +233,27 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                 const int i = __ffs(todo) - 1;
                 todo &= todo - 1;
                 const int ci = __shfl_sync(full, cnt, i);
-                const float4 ph = S.home[i];
-                const float dx = __fsub_rn(ph.x, pj.x);
-                const float dy = __fsub_rn(ph.y, pj.y);
-                const float dz = __fsub_rn(ph.z, pj.z);
-                float d2 = __fmul_rn(dx, dx);
-                d2 = __fmaf_rn(dy, dy, d2);
-                d2 = __fmaf_rn(dz, dz, d2);
-                bool acc = q < M && d2 < h2_lo;
-                const bool band = q < M && d2 >= h2_lo && d2 <= h2_hi;
-                if (__any_sync(full, band))
-                    if (band) acc = within_exact(ph.x, ph.y, ph.z, pj.x, pj.y, pj.z, h_d);
-                const unsigned mask = __ballot_sync(full, acc);
-                const int rank = ci + __popc(mask & lt);
-                if (acc && rank < cap) S.list[i][rank] = sj;
-                if (lane == i) cnt = ci + __popc(mask);
+                const ulonglong2 hxy = S.home_xy[i];
+                const f32x2 dx = f2sub(hxy.x, cx), dy = f2sub(hxy.y, cy), dz = f2sub(S.home_z[i], cz);
+                f32x2 d2p = f2mul(dx, dx);
+                d2p = f2fma(dy, dy, d2p);
+                d2p = f2fma(dz, dz, d2p);
+                float d20, d21;
+                f2unpack(d2p, d20, d21);
+                bool acc0 = v0 && d20 < h2_lo, acc1 = v1 && d21 < h2_lo;
+                const bool band0 = v0 && d20 >= h2_lo && d20 <= h2_hi;
+                const bool band1 = v1 && d21 >= h2_lo && d21 <= h2_hi;
+                if (__any_sync(full, band0 || band1)) {
+                    const float4 ph = S.home[i];
+                    if (band0) acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
+                    if (band1) acc1 = within_exact(ph.x, ph.y, ph.z, pj1.x, pj1.y, pj1.z, h_d);
+                }
+                const unsigned m0 = __ballot_sync(full, acc0), m1 = __ballot_sync(full, acc1);
+                const int n0 = __popc(m0);
+                const int r0 = ci + __popc(m0 & lt), r1 = ci + n0 + __popc(m1 & lt);
+                if (acc0 && r0 < cap) S.list[i][r0] = sj0;
+                if (acc1 && r1 < cap) S.list[i][r1] = sj1;
+                if (lane == i) cnt = ci + n0 + __popc(m1);
             }
         }
         __syncwarp();
