@@ -49,7 +49,7 @@ for _p in (os.path.join(ROOT, "cuda-sph_gb300"), ROOT):
 STAGE_BYTES_PER_PARTICLE = {"hash": 20, "scan": 0, "scatter": 8, "rank_gather": 48,
                             "density": 16, "force_integrate": 100, "step_counter": 0}
 STAGE_BYTES_PER_VOXEL = {"hash": 4, "scan": 8}
-KERNELS_PER_STEP = 9   # hash, 3 scan, scatter, rank-gather, density, force+integrate, counter
+KERNELS_PER_STEP = 10  # hash, 3 scan, scatter, big-voxel sort, rank-gather, density, force+integrate, counter
 
 
 _T0 = time.perf_counter()
@@ -73,9 +73,16 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched/served sections")
     ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=50)
+    ap.add_argument("--tuning", choices=["auto", "default"], default="auto",
+                    help="launch tuning: autotuned on the scene, or the library defaults")
     ap.add_argument("--served-requests", type=int, default=24)
     ap.add_argument("--served-rate", type=float, default=64.0, help="Poisson arrivals per second")
     return ap.parse_args()
+
+
+METRIC = {"config2": "particle-steps/s (4M box, 1 GB300)",
+          "box2m": "particle-steps/s (2M box, 1 GB300)",
+          "config0": "particle-steps/s (8k box, 1 GB300)"}
 
 
 def workload(name):
@@ -230,9 +237,12 @@ def run_gb300(args):
     n = spec.n
     log(f"workload {args.workload}: {n} particles")
     # launch tuning picked by the autotuner on this scene (results unchanged)
-    from sphgb.autotune import autotune, summary
-    best, tried = autotune([(spec, state)], steps=3, device=str(dev))
-    log(f"autotune: best {best}")
+    from sphgb.autotune import Tuning, autotune, summary
+    if args.tuning == "auto":
+        best, tried = autotune([(spec, state)], steps=3, device=str(dev))
+    else:
+        best, tried = Tuning(), []
+    log(f"tuning: {best}")
     batch = SceneBatch([spec], device=str(dev))
     best.apply(batch)
     batch.load_states([state])
@@ -316,8 +326,7 @@ def run_gb300(args):
            "api": "sphgb_compute_next_state_host"}
     assert np.isfinite(o_rho).all()
 
-    out = {"metric": "particle-steps/s (4M box, 1 GB300)" if args.workload == "config2"
-           else "particle-steps/s (8k box)",
+    out = {"metric": METRIC[args.workload],
            "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -422,25 +431,26 @@ def run_reference(args):
     sp = ref.params_from_spec(spec)
     pos = np.ascontiguousarray(state.position, dtype=np.float64)
     vel = np.ascontiguousarray(state.velocity, dtype=np.float64)
-    for s in range(min(args.warmup, 1)):
-        pos, vel, _ = ref.step(sp, pos, vel, step_index=s)
+    # like the GPU arm, every step is a full step of the same step-0 state
+    for _ in range(max(args.warmup, 0)):
+        ref.step(sp, pos, vel, step_index=0)
     t0 = time.perf_counter()
-    for s in range(args.steps):
-        pos, vel, _ = ref.step(sp, pos, vel, step_index=s)
+    for _ in range(args.steps):
+        ref.step(sp, pos, vel, step_index=0)
     dt = time.perf_counter() - t0
     value = spec.n * args.steps / dt
     cores = ref.num_threads()
     out = {"impl": "reference",
-           "metric": "particle-steps/s (4M box, 1 GB300)" if args.workload == "config2"
-           else "particle-steps/s (8k box)",
+           "metric": METRIC[args.workload],
            "value": value, "unit": "particle-steps/s", "n_gpus": int(os.environ.get("WORLD_SIZE", 1)),
-           "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": dt / args.steps * 1e3,
+           "steps": args.steps, "warmup": max(args.warmup, 0), "ms_per_step": dt / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic",
            "config": {"workload": desc, "particles": spec.n, "parallelism": "host cores"},
            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores,
                             "kind": "port",
-                            "sample": f"{args.steps} full steps of the {spec.n}-particle scene"},
+                            "sample": f"{args.steps} full steps of the {spec.n}-particle "
+                                      "scene's step-0 state"},
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)

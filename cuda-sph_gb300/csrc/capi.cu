@@ -1034,6 +1034,45 @@ int sphgb_philox_uniform(uint64_t seed, const int32_t* d_pid, int n, int step, i
     return SPHGB_OK;
 }
 
+int sphgb_generator_size(void) { return (int)sizeof(SphgbGenerator); }
+
+int sphgb_generate(const SphgbGenerator* g, const double* d_pipe, int pipe_rows, int64_t n,
+                   double* d_pos, double* d_vel, void* stream) {
+    if (!g) return fail(SPHGB_ERR_INVALID, "null generator");
+    if (n < 0 || n > (int64_t)INT32_MAX) return fail(SPHGB_ERR_RANGE, "particle count out of range");
+    if (n > 0 && (!d_pos || !d_vel)) return fail(SPHGB_ERR_INVALID, "null output");
+    switch (g->kind) {
+    case SPHGB_GEN_LATTICE:
+        if (g->lattice[0] <= 0 || g->lattice[1] <= 0 || g->lattice[2] <= 0 ||
+            (int64_t)g->lattice[0] * g->lattice[1] * g->lattice[2] != n)
+            return fail(SPHGB_ERR_INVALID, "lattice nx*ny*nz must equal n");
+        break;
+    case SPHGB_GEN_BOX_WALL:
+        break;
+    case SPHGB_GEN_PIPE_FILL:
+        if (!d_pipe || pipe_rows < 2)
+            return fail(SPHGB_ERR_INVALID, "pipe fill needs a pipe table of >= 2 rows");
+        break;
+    default:
+        return fail(SPHGB_ERR_INVALID, "unknown generator kind");
+    }
+    SPHGB_CUDA(launch_generate(*g, d_pipe, pipe_rows, n, d_pos, d_vel, as_stream(stream)));
+    return SPHGB_OK;
+}
+
+int sphgb_point_field(const float* d_pos, int pos_stride, const float* d_rho, int64_t n,
+                      const float* h_proj, const float* h_model, const float* h_view,
+                      float* d_clip_out, float* d_colour_out, float* d_size_out, void* stream) {
+    if (n < 0) return fail(SPHGB_ERR_INVALID, "bad size");
+    if (pos_stride < 3) return fail(SPHGB_ERR_INVALID, "position stride below 3 floats");
+    if (!h_proj || !h_model || !h_view) return fail(SPHGB_ERR_INVALID, "null matrix");
+    if (n > 0 && (!d_pos || !d_rho || !d_clip_out || !d_colour_out || !d_size_out))
+        return fail(SPHGB_ERR_INVALID, "null buffer");
+    SPHGB_CUDA(launch_point_field(d_pos, pos_stride, d_rho, n, h_proj, h_model, h_view, d_clip_out,
+                                  d_colour_out, d_size_out, as_stream(stream)));
+    return SPHGB_OK;
+}
+
 }  // extern "C"
 
 // ---- voxel organisation without allocation --------------------------------

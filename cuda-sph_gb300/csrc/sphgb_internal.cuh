@@ -19,6 +19,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+struct SphgbGenerator;   // include/sphgb.h
+
 namespace sphgb {
 
 constexpr int kBlock = 256;
@@ -416,5 +418,12 @@ cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t*
                               const int32_t* vcount, int32_t* list, int stride,
                               int32_t* n_capped, int32_t* n_uncapped);
 cudaError_t launch_aux_from_rho(const Launch& L, const float* rho, float2* aux);
+
+// generate.cu: start states and the point-field vertex stage
+cudaError_t launch_generate(const SphgbGenerator& g, const double* pipe, int pipe_rows, int64_t n,
+                            double* pos, double* vel, cudaStream_t st);
+cudaError_t launch_point_field(const float* pos, int stride, const float* rho, int64_t n,
+                               const float* proj16, const float* model16, const float* view16,
+                               float* clip, float* colour, float* size, cudaStream_t st);
 
 }  // namespace sphgb

@@ -55,6 +55,27 @@ class SceneParams(C.Structure):
     ]
 
 
+GEN_LATTICE, GEN_BOX_WALL, GEN_PIPE_FILL = 0, 1, 2
+
+
+class Generator(C.Structure):
+    """SphgbGenerator (include/sphgb.h)."""
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("lattice", C.c_int32 * 3),
+        ("spacing", C.c_double),
+        ("jitter", C.c_double),
+        ("origin", C.c_double * 3),
+        ("extent", C.c_double * 3),
+        ("velocity", C.c_double * 3),
+        ("velocity_spread", C.c_double),
+        ("velocity_sigma", C.c_double),
+        ("x_range", C.c_double * 2),
+        ("fill", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
 # (name, restype, argtypes) for every entry point declared in include/sphgb.h
 _VP, _I, _I64, _U64 = C.c_void_p, C.c_int, C.c_int64, C.c_uint64
 SIGNATURES = [
@@ -87,6 +108,9 @@ SIGNATURES = [
     ("sphgb_pipe_x_at_segment_beginning", _I, [_VP, _I, _VP, _I, _VP, _VP]),
     ("sphgb_pipe_solve_collision", _I, [_VP, _VP, _I, _VP, _I, _VP, _VP]),
     ("sphgb_philox_uniform", _I, [_U64, _VP, _I, _I, _I, _VP, _VP]),
+    ("sphgb_generator_size", _I, []),
+    ("sphgb_generate", _I, [C.POINTER(Generator), _VP, _I, _I64, _VP, _VP, _VP]),
+    ("sphgb_point_field", _I, [_VP, _I, _VP, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 ]
 
 _lib = None
@@ -119,6 +143,8 @@ def load(build_if_missing: bool = False):
         raise OSError("libsphgb ABI version mismatch")
     if L.sphgb_scene_params_size() != C.sizeof(SceneParams):
         raise OSError("SphgbSceneParams layout mismatch between libsphgb.so and the binding")
+    if L.sphgb_generator_size() != C.sizeof(Generator):
+        raise OSError("SphgbGenerator layout mismatch between libsphgb.so and the binding")
     _lib = L
     return L
 

@@ -262,6 +262,67 @@ int sphgb_philox_uniform(uint64_t seed, const int32_t* d_pid, int n, int step, i
 
 #endif /* SPHGB_NO_FUNCTIONS */
 
+/* ---- initial states on the device --------------------------------------
+ * Replaces the host start-state loops of config.py:79-121
+ * (__start_state_box_wall, __start_state_inside_pipe) and the reference's
+ * spawn_particles_inside_pipe_kernel (sim/src/sph/kernels/base_kernels.py:
+ * 130-143); LATTICE is the jittered dam-break block of the benchmark scenes.
+ * Random numbers: Philox4x32-10 uniforms u(draw) = sphgb_philox_uniform(seed,
+ * i, step = -1, draw) for particle i, so a state depends only on (generator,
+ * n) and not on the launch shape.  Normal deviates use the Box-Muller
+ * transform sqrt(-2 ln(1 - u(d))) cos(2 pi u(d + 1)).  Output: FP64 (n, 3)
+ * position and velocity in particle-id order, ready for
+ * sphgb_ctx_load_aos_f64. */
+enum { SPHGB_GEN_LATTICE = 0, SPHGB_GEN_BOX_WALL = 1, SPHGB_GEN_PIPE_FILL = 2 };
+
+typedef struct SphgbGenerator {
+    int32_t kind;              /* SPHGB_GEN_* */
+    int32_t lattice[3];        /* LATTICE: nx, ny, nz; n must be nx*ny*nz; particle
+                                  i = (ix*ny + iy)*nz + iz (C order of the index grid) */
+    double spacing;            /* LATTICE: p = origin + (idx + 0.5)*spacing + jitter*(2u - 1),
+                                  u = draws 0, 1, 2 */
+    double jitter;
+    double origin[3];
+    double extent[3];          /* BOX_WALL: p = u * extent, draws 0, 1, 2 (config.py:81-88 uses
+                                  (0.1*space_x, space_y, space_z)) */
+    double velocity[3];        /* every kind: base velocity */
+    double velocity_spread;    /* BOX_WALL: v = velocity + (u - 0.5)*spread, draws 3, 4, 5
+                                  (config.py:89-95: base (1.5, -5, -5), spread 1) */
+    double velocity_sigma;     /* LATTICE, PIPE_FILL: v = velocity + sigma*N(0,1) per axis,
+                                  normal draws (3,4), (5,6), (7,8); 0 = velocity exactly */
+    double x_range[2];         /* PIPE_FILL: x = x0 + u*(x1 - x0), draw 0 (config.py:104: [0, length)) */
+    double fill;               /* PIPE_FILL: r = sqrt(u)*R(x)*fill, draw 1, with R the pipe radius of
+                                  calc_radius_in_position (util_kernels.py:56-69); theta =
+                                  u*2*pi, draw 2; (y, z) = axis of row 0 + r (cos, sin) theta
+                                  (config.py:107-111: fill 0.98; base_kernels.py:102-112: 1) */
+    uint64_t seed;
+} SphgbGenerator;
+
+#ifndef SPHGB_NO_FUNCTIONS
+
+int sphgb_generator_size(void);   /* sizeof(SphgbGenerator), for binding checks */
+/* d_pipe / pipe_rows: the Pipe.to_numpy table on the device (PIPE_FILL only;
+ * NULL / 0 otherwise).  x outside the table's rows takes the radius of the
+ * first segment. */
+int sphgb_generate(const SphgbGenerator* gen, const double* d_pipe, int pipe_rows, int64_t n,
+                   double* d_pos, double* d_vel, void* stream);
+
+/* ---- point-field vertex stage, headless --------------------------------
+ * The arithmetic of the visualiser's shaders (vis/assets/point_field.vert:
+ * 14-23, point_field.frag:5-9) per particle, written to device buffers
+ * instead of a window: clip = (((P V) M) (x, y, z, 1)) with the 4x4 product
+ * PVM = (P V) M formed once (column-major like GLSL uniforms, FP32, each
+ * element summed k = 0..3 with one rounding per multiply and add);
+ * t = min(rho / 10, 1); colour = (0.1, 0.7, 0.5)(1 - t) + (0.7 (0.3, 0.4, 1)) t,
+ * alpha 0.5; point size = min(max(1, (40 + (1 - t) 20) / clip.z), 13).
+ * min and max ignore a NaN operand (fminf / fmaxf).  d_pos has pos_stride
+ * floats per particle (3 = packed vertex buffer, 4 = the library's float4). */
+int sphgb_point_field(const float* d_pos, int pos_stride, const float* d_rho, int64_t n,
+                      const float* h_proj, const float* h_model, const float* h_view,
+                      float* d_clip_out, float* d_colour_out, float* d_size_out, void* stream);
+
+#endif /* SPHGB_NO_FUNCTIONS */
+
 #ifdef __cplusplus
 }
 #endif

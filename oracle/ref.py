@@ -63,6 +63,27 @@ def make_params(*, n, space_size, voxel_size, external_force, dt, mass, rho_0, i
     return sp
 
 
+GEN_LATTICE, GEN_BOX_WALL, GEN_PIPE_FILL = 0, 1, 2
+
+
+class Generator(C.Structure):
+    """Same layout as SphgbGenerator in include/sphgb.h."""
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("lattice", C.c_int32 * 3),
+        ("spacing", C.c_double),
+        ("jitter", C.c_double),
+        ("origin", C.c_double * 3),
+        ("extent", C.c_double * 3),
+        ("velocity", C.c_double * 3),
+        ("velocity_spread", C.c_double),
+        ("velocity_sigma", C.c_double),
+        ("x_range", C.c_double * 2),
+        ("fill", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+
 _lib = None
 
 
@@ -95,6 +116,9 @@ def lib():
         L.ref_is_out_of_pipe.argtypes = [d, d, C.c_int]
         L.ref_solve_collision.argtypes = [d, d, d, C.c_int]
         L.ref_collide_pipe_one.argtypes = [d, d, d, C.c_int, C.c_uint64, C.c_int32, C.c_int32]
+        f32 = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.ref_generate.argtypes = [P(Generator), vp, C.c_int, C.c_int64, d, d]
+        L.ref_point_field.argtypes = [f32, C.c_int, f32, C.c_int64, f32, f32, f32, f32, f32, f32]
         L.ref_num_threads.restype = C.c_int
         L.ref_set_num_threads.argtypes = [C.c_int]
         _lib = L
@@ -214,6 +238,30 @@ def solve_collision(p, v, pipe, seg):
     p, v = _c(p).copy(), _c(v).copy()
     lib().ref_solve_collision(p, v, _c(pipe), int(seg))
     return p, v
+
+
+def generate(gen, n, pipe=None):
+    """Start state (pos, vel) FP64 (n, 3) of the generator (ref_cpu.c ref_generate)."""
+    pos = np.empty((n, 3)); vel = np.empty((n, 3))
+    table = None if pipe is None else _c(pipe)
+    rows = 0 if pipe is None else len(table)
+    ptr = None if table is None else table.ctypes.data_as(C.c_void_p)
+    rc = lib().ref_generate(C.byref(gen), ptr, rows, int(n), pos, vel)
+    if rc != 0:
+        raise ValueError("invalid generator")
+    return pos, vel
+
+
+def point_field(pos, stride, rho, proj, model, view):
+    """(clip (n,4), colour (n,4), size (n,)) FP32 of the point-field vertex stage."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1)
+    rho = np.ascontiguousarray(rho, dtype=np.float32)
+    n = len(rho)
+    m = [np.ascontiguousarray(x, dtype=np.float32).reshape(16) for x in (proj, model, view)]
+    clip = np.empty((n, 4), np.float32); col = np.empty((n, 4), np.float32)
+    size = np.empty(n, np.float32)
+    lib().ref_point_field(pos, int(stride), rho, n, m[0], m[1], m[2], clip, col, size)
+    return clip, col, size
 
 
 def num_threads():

@@ -418,8 +418,8 @@ void ref_collide_pipe_one(double* p, double* v, const double* pipe, int rows,
             double R = ref_radius_in_position(p, pipe, s);
             double r = R * sqrt(ref_philox_uniform(seed, pid, step, 0));
             double th = ref_philox_uniform(seed, pid, step, 1) * 2.0 * PI;
-            p[1] = P(0, 1) + r * cos(th);
-            p[2] = P(0, 2) + r * sin(th);
+            p[1] = pipe[1] + r * cos(th);     /* row 0: [x0, y0, z0, r, len] */
+            p[2] = pipe[2] + r * sin(th);
         }
     } else if (ref_is_out_of_pipe(p, pipe, seg)) {
         ref_solve_collision(p, v, pipe, seg);
@@ -500,4 +500,101 @@ void ref_set_num_threads(int n) {
 #else
     (void)n;
 #endif
+}
+
+/* ---- start states (config.py:79-121; base_kernels.py:102-112, 130-143) --
+ * Same draws and operation order as the library's generator: Philox uniforms
+ * keyed (seed, particle id) with counter word 1 = 0xFFFFFFFF. */
+static double gen_u(uint64_t seed, int64_t i, int draw) {
+    return ref_philox_uniform(seed, (int32_t)(uint32_t)i, -1, draw);
+}
+
+/* Box-Muller (Box and Muller, 1958) */
+static double gen_normal(uint64_t seed, int64_t i, int d) {
+    double u1 = 1.0 - gen_u(seed, i, d);
+    double u2 = gen_u(seed, i, d + 1);
+    double r = sqrt(-2.0 * log(u1));
+    return r * cos(u2 * 2.0 * PI);
+}
+
+int ref_generate(const SphgbGenerator* g, const double* pipe, int rows, int64_t n, double* pos,
+                 double* vel) {
+    if (g->kind == SPHGB_GEN_LATTICE &&
+        (int64_t)g->lattice[0] * g->lattice[1] * g->lattice[2] != n)
+        return -1;
+    if (g->kind == SPHGB_GEN_PIPE_FILL && (!pipe || rows < 2)) return -1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double p[3], v[3];
+        int normal_v = 0;
+        if (g->kind == SPHGB_GEN_LATTICE) {
+            int64_t ny = g->lattice[1], nz = g->lattice[2];
+            int64_t idx[3] = {i / (ny * nz), (i / nz) % ny, i % nz};
+            for (int a = 0; a < 3; ++a) {
+                double base = g->origin[a] + ((double)idx[a] + 0.5) * g->spacing;
+                p[a] = base + g->jitter * (2.0 * gen_u(g->seed, i, a) - 1.0);
+                v[a] = g->velocity[a];
+            }
+            normal_v = g->velocity_sigma != 0.0;
+        } else if (g->kind == SPHGB_GEN_BOX_WALL) {
+            for (int a = 0; a < 3; ++a) {
+                p[a] = gen_u(g->seed, i, a) * g->extent[a];
+                v[a] = g->velocity[a] + (gen_u(g->seed, i, 3 + a) - 0.5) * g->velocity_spread;
+            }
+        } else {
+            p[0] = g->x_range[0] + gen_u(g->seed, i, 0) * (g->x_range[1] - g->x_range[0]);
+            p[1] = p[2] = 0.0;
+            int seg = ref_find_segment(p, pipe, rows);
+            if (seg < 0) seg = 0;
+            double R = ref_radius_in_position(p, pipe, seg);
+            double r = sqrt(gen_u(g->seed, i, 1)) * R * g->fill;
+            double th = gen_u(g->seed, i, 2) * 2.0 * PI;
+            p[1] = pipe[1] + r * cos(th);     /* row 0: [x0, y0, z0, r, len] */
+            p[2] = pipe[2] + r * sin(th);
+            for (int a = 0; a < 3; ++a) v[a] = g->velocity[a];
+            normal_v = g->velocity_sigma != 0.0;
+        }
+        if (normal_v)
+            for (int a = 0; a < 3; ++a) v[a] += g->velocity_sigma * gen_normal(g->seed, i, 3 + 2 * a);
+        for (int a = 0; a < 3; ++a) {
+            pos[3 * i + a] = p[a];
+            vel[3 * i + a] = v[a];
+        }
+    }
+    return 0;
+}
+
+/* ---- point-field vertex stage (vis/assets/point_field.vert:14-23) ------ */
+static void mat_mul(const float* a, const float* b, float* out) {   /* column-major */
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            float s = a[r] * b[c * 4];
+            for (int k = 1; k < 4; ++k) s = s + a[k * 4 + r] * b[c * 4 + k];
+            out[c * 4 + r] = s;
+        }
+}
+
+void ref_point_field(const float* pos, int stride, const float* rho, int64_t n, const float* proj,
+                     const float* model, const float* view, float* clip, float* colour,
+                     float* size) {
+    float pv[16], m[16];
+    mat_mul(proj, view, pv);
+    mat_mul(pv, model, m);
+    const float b0 = 0.3f * 0.7f, b1 = 0.4f * 0.7f, b2 = 0.7f;
+    for (int64_t i = 0; i < n; ++i) {
+        const float x[4] = {pos[i * stride], pos[i * stride + 1], pos[i * stride + 2], 1.0f};
+        for (int r = 0; r < 4; ++r) {
+            float s = m[r] * x[0];
+            for (int k = 1; k < 4; ++k) s = s + m[k * 4 + r] * x[k];
+            clip[4 * i + r] = s;
+        }
+        float t = fminf(rho[i] / 10.0f, 1.0f);
+        float omt = 1.0f - t;
+        colour[4 * i + 0] = 0.1f * omt + b0 * t;
+        colour[4 * i + 1] = 0.7f * omt + b1 * t;
+        colour[4 * i + 2] = 0.5f * omt + b2 * t;
+        colour[4 * i + 3] = 0.5f;
+        float big = 40.0f + omt * 20.0f;
+        size[i] = fminf(fmaxf(1.0f, big / clip[4 * i + 2]), 13.0f);
+    }
 }

@@ -141,3 +141,31 @@ def test_trajectory_config0_200_steps():
         elif step == 100:
             assert med < 1e-5
     b.close()
+
+
+def test_conservation_sums_match_fp64_sums_of_the_state():
+    """sphgb_ctx_conservation (FP64, fixed order) against numpy FP64 sums of
+    the same state: relative 1e-12 (only the summation order differs)."""
+    torch_cuda()
+    from sphgb import scenes
+    from sphgb.device import SceneBatch
+    specs = [scenes.config0(), scenes.pipe_flow(n=20_000, seed=11,
+                                                h=0.02 * (262_144 / 20_000) ** (1 / 3))]
+    b = SceneBatch([s for s, _ in specs])
+    b.load_states([st for _, st in specs])
+    b.step(3)
+    cons = b.conservation()
+    for k, (spec, _) in enumerate(specs):
+        st = b.states()[k]
+        m = np.float64(np.float32(spec.constants.mass))
+        g = np.asarray(spec.params.external_force, dtype=np.float32).astype(np.float64)
+        v2 = (st.velocity ** 2).sum(1)
+        want = [m * spec.n, *(m * st.velocity.sum(0)), 0.5 * m * v2.sum(),
+                -m * (st.position @ g).sum()]
+        want += [want[4] + want[5], spec.n]
+        scale = [abs(w) if w != 0 else 1.0 for w in want]
+        scale[1:4] = [m * np.abs(st.velocity).sum()] * 3
+        scale[5] = scale[6] = m * np.abs(st.position @ g).sum() + 0.5 * m * v2.sum() + 1e-300
+        err = np.abs(cons[k] - np.asarray(want)) / np.asarray(scale)
+        assert err.max() < 1e-12, (k, cons[k], want)
+    b.close()
