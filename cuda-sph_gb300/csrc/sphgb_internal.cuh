@@ -405,6 +405,10 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vs
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
                               const int2* tasks, const int32_t* task_count);
+// the same with 8 lanes per particle and 8 candidates per lane
+cudaError_t launch_density_tiled(const Launch& L, const float4* pos, const int32_t* vstart,
+                                 const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
+                                 const int2* tasks, const int32_t* task_count);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float2* aux, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);

@@ -5,7 +5,7 @@ Lattice and box-wall states use only Philox uniforms, additions and
 multiplications: bit-identical to the oracle.  The pipe fill and normal
 deviates call cos, sin and log, whose last bit may differ between CUDA's and
 the C library's implementations: positions within 1e-15 m (radii ~0.1 m,
-about 10 ulp), velocities within 1e-14 m/s.  The point field is FP32 with one
+about 10 ulp) or 2e-15 relative, velocities within 1e-14 m/s.  The point field is FP32 with one
 rounding per operation in both: bit-identical.
 """
 import numpy as np
@@ -18,6 +18,7 @@ pytestmark = pytest.mark.gpu
 
 TOL_TRIG_POS = 1e-15    # absolute, metres
 TOL_TRIG_VEL = 1e-14    # absolute, m/s
+TOL_TRIG_REL = 2e-15    # relative, for coordinates far from 1 (about 8 ulp)
 
 
 def _np(t):
@@ -78,7 +79,8 @@ def test_pipe_fill_matches_oracle_and_stays_inside():
     rp, rv = ref.generate(_oracle_gen(g), n, pipe=pipe.to_numpy())
     gp = _np(pos)
     np.testing.assert_array_equal(gp[:, 0], rp[:, 0])
-    np.testing.assert_allclose(gp, rp, rtol=0, atol=TOL_TRIG_POS)
+    # radii ~10 here: a few ulp of the coordinate
+    np.testing.assert_allclose(gp, rp, rtol=TOL_TRIG_REL, atol=0)
     np.testing.assert_array_equal(_np(vel), rv)
     table = pipe.to_numpy()
     for k in range(0, n, 997):

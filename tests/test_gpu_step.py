@@ -145,27 +145,80 @@ def test_trajectory_config0_200_steps():
 
 def test_conservation_sums_match_fp64_sums_of_the_state():
     """sphgb_ctx_conservation (FP64, fixed order) against numpy FP64 sums of
-    the same state: relative 1e-12 (only the summation order differs)."""
+    the same state: relative 1e-12 (only the summation order differs).  Two
+    boxes after three steps and a pipe flow as loaded (the pipe's FP64
+    position accumulator is what is summed)."""
     torch_cuda()
     from sphgb import scenes
     from sphgb.device import SceneBatch
-    specs = [scenes.config0(), scenes.pipe_flow(n=20_000, seed=11,
-                                                h=0.02 * (262_144 / 20_000) ** (1 / 3))]
-    b = SceneBatch([s for s, _ in specs])
-    b.load_states([st for _, st in specs])
-    b.step(3)
-    cons = b.conservation()
-    for k, (spec, _) in enumerate(specs):
-        st = b.states()[k]
-        m = np.float64(np.float32(spec.constants.mass))
-        g = np.asarray(spec.params.external_force, dtype=np.float32).astype(np.float64)
-        v2 = (st.velocity ** 2).sum(1)
-        want = [m * spec.n, *(m * st.velocity.sum(0)), 0.5 * m * v2.sum(),
-                -m * (st.position @ g).sum()]
-        want += [want[4] + want[5], spec.n]
-        scale = [abs(w) if w != 0 else 1.0 for w in want]
-        scale[1:4] = [m * np.abs(st.velocity).sum()] * 3
-        scale[5] = scale[6] = m * np.abs(st.position @ g).sum() + 0.5 * m * v2.sum() + 1e-300
-        err = np.abs(cons[k] - np.asarray(want)) / np.asarray(scale)
-        assert err.max() < 1e-12, (k, cons[k], want)
-    b.close()
+    boxes = [scenes.config0(), scenes.box_dam_break(nx=10, ny=20, nz=10, seed=4,
+                                                   gravity=(1.0, -9.0, 3.0))]
+    pipe = [scenes.pipe_flow(n=20_000, seed=11, h=0.02 * (262_144 / 20_000) ** (1 / 3))]
+    for pairs, steps in ((boxes, 3), (pipe, 0)):
+        b = SceneBatch([s for s, _ in pairs])
+        b.load_states([st for _, st in pairs])
+        b.step(steps)
+        cons = b.conservation()
+        states = b.states()
+        for k, (spec, _) in enumerate(pairs):
+            st = states[k]
+            assert np.isfinite(st.position).all() and np.isfinite(st.velocity).all()
+            m = np.float64(np.float32(spec.constants.mass))
+            g = np.asarray(spec.params.external_force, dtype=np.float32).astype(np.float64)
+            v2 = (st.velocity ** 2).sum(1)
+            pot = -m * (st.position @ g)
+            want = np.array([m * spec.n, *(m * st.velocity.sum(0)), 0.5 * m * v2.sum(),
+                             pot.sum(), 0.5 * m * v2.sum() + pot.sum(), spec.n])
+            scale = np.array([m * spec.n] + [m * np.abs(st.velocity).sum() + 1e-300] * 3
+                             + [0.5 * m * v2.sum() + 1e-300] + [np.abs(pot).sum() + 1e-300]
+                             + [np.abs(pot).sum() + 0.5 * m * v2.sum() + 1e-300] + [spec.n])
+            err = np.abs(cons[k] - want) / scale
+            assert err.max() < 1e-12, (k, cons[k], want)
+        b.close()
+
+
+@pytest.mark.parametrize("name", ["config0", "pipe", "uncapped", "truncated"])
+def test_density_variants_bit_identical(name):
+    """The three density kernels (lane per candidate, 8 lanes per particle,
+    thread per particle) keep the same neighbours in the same order and sum
+    them the same way: identical states after several steps."""
+    torch_cuda()
+    from sphgb import _capi
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()[name]
+    outs = []
+    for variant in (_capi.DENSITY_WARP, _capi.DENSITY_TILED, _capi.DENSITY_THREAD):
+        b = SceneBatch([spec])
+        b.set_tuning(256, variant, 64)
+        b.load_states([st])
+        b.step(4, use_graph=True)
+        outs.append(b.states()[0])
+        b.close()
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o.density, outs[0].density)
+        np.testing.assert_array_equal(o.velocity, outs[0].velocity)
+        np.testing.assert_array_equal(o.position, outs[0].position)
+
+
+def test_density_variants_identical_on_dense_voxels():
+    """Voxels far above 32 particles (many tasks per voxel, thousands of
+    candidates per walk, several staged chunks) and a scene whose block
+    starts at a voxel boundary."""
+    torch_cuda()
+    from sphgb import _capi, scenes
+    from sphgb.device import SceneBatch
+    cases = [scenes.box_dam_break(nx=24, ny=24, nz=24, spacing=0.004, jitter=0.0004,
+                                  h=0.03, mass=6.4e-5, seed=12),
+             scenes.pipe_flow(n=30_000, seed=13, h=0.02)]
+    for spec, st in cases:
+        outs = []
+        for variant in (_capi.DENSITY_WARP, _capi.DENSITY_TILED, _capi.DENSITY_THREAD):
+            b = SceneBatch([spec])
+            b.set_tuning(256, variant, 64)
+            b.load_states([st])
+            b.step(2)
+            outs.append(b.states()[0])
+            b.close()
+        for o in outs[1:]:
+            np.testing.assert_array_equal(o.density, outs[0].density)
+            np.testing.assert_array_equal(o.velocity, outs[0].velocity)
