@@ -372,8 +372,16 @@ struct Launch {
     bool pipe_scenes;           // some scene is in pipe mode
     int sort_block = kBlock;    // threads per block of the per-particle sort kernels
     int big_voxel = 64;         // voxels above this many members are sorted per block
+    int task_kind = 0;          // density tasks the rank-gather emits (kTask*)
     cudaStream_t stream;
 };
+
+// density tasks: kTaskRuns = (voxel, first slot) per run of <= 32 slots of a
+// voxel; kTaskRows = (first voxel of a row chunk, scene) per occupied chunk of
+// kRowX voxels along x, or (overflow voxel, ~scene) for a scene's overflow bucket
+constexpr int kTaskRuns = 0;
+constexpr int kTaskRows = 1;
+constexpr int kRowX = 16;
 
 // cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow bucket
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
@@ -405,6 +413,11 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vs
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
                               const int2* tasks, const int32_t* task_count);
+// one block per row chunk: the chunk's 27-voxel neighbourhood staged in shared
+// memory, one thread per particle
+cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_t* vstart,
+                                const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
+                                const int2* tasks, const int32_t* task_count);
 // the same with 8 lanes per particle and 8 candidates per lane
 cudaError_t launch_density_tiled(const Launch& L, const float4* pos, const int32_t* vstart,
                                  const int32_t* vcount, float* rho, float2* aux, NbrList nbr,

@@ -289,6 +289,181 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
     }
 }
 
+// Row-chunk density pass.  A task is a chunk of kRowX consecutive voxels of one
+// row of the voxel table (fixed y, z; x fastest, so the chunk's particles are
+// consecutive slots).  Every walk voxel of its particles lies in one of 9 row
+// segments (y +-1, z +-1) spanning x0 - 1 .. x0 + kRowX, each again a run of
+// consecutive slots, so the block copies the whole neighbourhood into shared
+// memory with 9 coalesced copies.  Then one thread per particle walks its 27
+// voxels from shared memory exactly like walk() (same order, voxel culling,
+// FP32 test with the FP64 guard band, cap with self counted), summing its
+// density in walk order as it accepts neighbours and writing its neighbour
+// list.  Results are bit-identical to density_one.  Scenes in truncated-walk
+// mode or with a cap beyond the list, neighbourhoods beyond the shared
+// buffer and overflow buckets take density_one (global memory walk).
+// density_one out of line: the fallback paths of the row kernel keep their
+// registers out of its fast path
+__device__ __noinline__ void density_one_call(int s, const SceneDev& sc,
+                                              const float4* __restrict__ pos,
+                                              const int32_t* __restrict__ vstart,
+                                              const int32_t* __restrict__ vcount, int n,
+                                              float* __restrict__ rho, float2* __restrict__ aux,
+                                              NbrList nbr, int32_t* row, int stride) {
+    density_one(s, __ldg(pos + s), sc, pos, vstart, vcount, n, rho, aux, nbr, row, stride);
+}
+
+constexpr int kRowThreads = 256;
+constexpr int kRowStage = 2560;                 // staged particles (40 KB)
+constexpr int kRowSpan = kRowX + 2;             // x0 - 1 .. x0 + kRowX
+
+struct RowShared {
+    float4 pos[kRowStage];
+    int32_t vs[9][kRowSpan];    // start slot of each walk voxel of the chunk
+    int32_t vc[9][kRowSpan];    // member count (0 outside the table)
+    int32_t len[9], slot0[9], base[9];
+    int32_t fallback;
+};
+
+__global__ void __launch_bounds__(kRowThreads, 4)
+k_density_rows(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+               int n_scenes, int n, const float4* __restrict__ pos,
+               const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+               float* __restrict__ rho, float2* __restrict__ aux, NbrList nbr,
+               const int2* __restrict__ tasks, const int32_t* __restrict__ task_count) {
+    __shared__ RowShared S;
+    // per-thread list scratch of density_one (kListCap rows of kRowThreads)
+    int32_t* scratch = reinterpret_cast<int32_t*>(S.pos) + threadIdx.x;
+    static_assert(kListCap * kRowThreads * 4 <= (int)sizeof(S.pos), "scratch fits the stage");
+    const int n_tasks = *task_count;
+    for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
+        const int2 task = tasks[t];
+        __syncthreads();                        // the previous task is done with S
+        if (task.y < 0) {                       // overflow bucket: non-finite particles
+            const SceneDev& sc = scenes[~task.y];
+            const int st = __ldg(vstart + task.x), c = __ldg(vcount + task.x);
+            for (int s = st + threadIdx.x; s < st + c; s += blockDim.x)
+                density_one_call(s, sc, pos, vstart, vcount, n, rho, aux, nbr, scratch, kRowThreads);
+            continue;
+        }
+        const SceneDev& sc = scenes[task.y];
+        const int D0 = sc.dims[0], D1 = sc.dims[1], D2 = sc.dims[2];
+        const int cv = task.x - sc.v_begin;
+        const int x0 = cv % D0, y = (cv / D0) % D1, z = cv / (D0 * D1);
+        const int x1 = min(x0 + kRowX, D0);     // chunk voxels x0 .. x1 - 1
+        const int S0 = __ldg(vstart + task.x);
+        const int S1 = __ldg(vstart + task.x + (x1 - 1 - x0)) + __ldg(vcount + task.x + (x1 - 1 - x0));
+        if (threadIdx.x < 9) {
+            const int k = threadIdx.x;
+            const int ny = y + k / 3 - 1, nz = z + k % 3 - 1;
+            int len = 0, s0 = 0;
+            if (ny >= 0 && ny < D1 && nz >= 0 && nz < D2) {
+                const int row = sc.v_begin + ny * D0 + nz * D0 * D1;
+                const int xa = max(x0 - 1, 0), xb = min(x1, D0 - 1);
+                s0 = __ldg(vstart + row + xa);
+                len = __ldg(vstart + row + xb) + __ldg(vcount + row + xb) - s0;
+            }
+            S.len[k] = len;
+            S.slot0[k] = s0;
+        }
+        for (int i = threadIdx.x; i < 9 * kRowSpan; i += blockDim.x) {
+            const int k = i / kRowSpan, xo = i % kRowSpan;
+            const int nx = x0 - 1 + xo, ny = y + k / 3 - 1, nz = z + k % 3 - 1;
+            int vs = 0, vc = 0;
+            if (nx >= 0 && nx < D0 && ny >= 0 && ny < D1 && nz >= 0 && nz < D2) {
+                const int vid = sc.v_begin + nx + ny * D0 + nz * D0 * D1;
+                vs = __ldg(vstart + vid);
+                vc = __ldg(vcount + vid);
+            }
+            S.vs[k][xo] = vs;
+            S.vc[k][xo] = vc;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int off = 0;
+            for (int k = 0; k < 9; ++k) {
+                S.base[k] = off - S.slot0[k];
+                off += S.len[k];
+            }
+            S.fallback = off > kRowStage || sc.walk_trunc || sc.cap > kListCap;
+        }
+        __syncthreads();
+        if (S.fallback) {
+            for (int s = S0 + threadIdx.x; s < S1; s += blockDim.x)
+                density_one_call(s, sc, pos, vstart, vcount, n, rho, aux, nbr, scratch, kRowThreads);
+            continue;
+        }
+        for (int k = 0; k < 9; ++k) {
+            const int len = S.len[k], s0 = S.slot0[k], b = S.base[k] + s0;
+            for (int i = threadIdx.x; i < len; i += blockDim.x) S.pos[b + i] = __ldg(pos + s0 + i);
+        }
+        __syncthreads();
+        const float vs0 = sc.vs[0], vs1 = sc.vs[1], vs2 = sc.vs[2];
+        const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi, cull2 = sc.cull2;
+        const double h_d = sc.h_d;
+        const int cap = sc.cap;
+        const float inv_h2 = 1.0f / sc.h2;
+        for (int s = S0 + threadIdx.x; s < S1; s += blockDim.x) {
+            const float4 pi = S.pos[S.base[4] + s];
+            Kahan acc;
+            int others = 0;
+            if (finite3(pi)) {
+                const int cx = voxel_coord(pi.x, vs0, D0);
+                // squared distances to the own voxel's faces (the culling of walk())
+                const float fx = pi.x - (float)cx * vs0;
+                const float fy = pi.y - (float)y * vs1;
+                const float fz = pi.z - (float)z * vs2;
+                const float gx0 = fx * fx, gx2 = (vs0 - fx) * (vs0 - fx);
+                const float gy0 = fy * fy, gy2 = (vs1 - fy) * (vs1 - fy);
+                const float gz0 = fz * fz, gz2 = (vs2 - fz) * (vs2 - fz);
+                int na = 0;
+#pragma unroll 1
+                for (int ddx = 0; ddx < 3; ++ddx) {
+                    const int nx = cx + ddx - 1;
+                    if (nx < 0 || nx >= D0) continue;
+                    const int xo = nx - x0 + 1;
+                    const float gx = ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f);
+#pragma unroll 1
+                    for (int ddy = 0; ddy < 3; ++ddy) {
+                        const float gxy = gx + (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
+#pragma unroll 1
+                        for (int ddz = 0; ddz < 3; ++ddz) {
+                            if (gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > cull2) continue;
+                            const int k = ddy * 3 + ddz;
+                            const int c = S.vc[k][xo];
+                            const int j0 = S.vs[k][xo];
+                            const float4* sp = S.pos + S.base[k];
+#pragma unroll 2
+                            for (int m = 0; m < c; ++m) {
+                                const int j = j0 + m;
+                                const float4 pj = sp[j];
+                                float dx, dy, dz, d2;
+                                if (within(pi, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2)) {
+                                    if (j != s) {
+                                        // d2 is the density sum's own distance arithmetic
+                                        const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                                        acc.add(u * u * u);
+                                        if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
+                                        ++others;
+                                    }
+                                    if (++na >= cap) goto walked;
+                                }
+                            }
+                        }
+                    }
+                }
+            walked:;
+            }
+            const float r = (acc.s * sc.w_const) * sc.mass;
+            rho[s] = r;
+            if (aux) {
+                const float p = sc.k * (r - sc.rho0);
+                aux[s] = make_float2(p / (r * r), 1.0f / r);
+            }
+            if (nbr.count) nbr.count[s] = others;
+        }
+    }
+}
+
 // Tiled density pass: one warp per task as above, but the warp is split into
 // four 8-lane segments, each serving one home particle, and each lane tests 8
 // consecutive candidates of the walk per batch (64 per home per batch).  The
@@ -771,6 +946,19 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t*
     k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                          vstart, vcount, rho, aux, nbr, tasks,
                                                          task_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_t* vstart,
+                                const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
+                                const int2* tasks, const int32_t* task_count) {
+    if (L.n == 0) return cudaSuccess;
+    // persistent grid: 4 blocks of 256 threads per SM, blocks stride over the chunks
+    int blocks = (L.n + 127) / 128;
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    k_density_rows<<<blocks, kRowThreads, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
+                                                          vstart, vcount, rho, aux, nbr, tasks,
+                                                          task_count);
     return cudaGetLastError();
 }
 

@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 TOL_TRIG_POS = 1e-15    # absolute, metres
 TOL_TRIG_VEL = 1e-14    # absolute, m/s
-TOL_TRIG_REL = 2e-15    # relative, for coordinates far from 1 (about 8 ulp)
+TOL_TRIG_REL = 2e-15    # relative to the pipe radius, for radii far from 1 (about 8 ulp)
 
 
 def _np(t):
@@ -79,8 +79,8 @@ def test_pipe_fill_matches_oracle_and_stays_inside():
     rp, rv = ref.generate(_oracle_gen(g), n, pipe=pipe.to_numpy())
     gp = _np(pos)
     np.testing.assert_array_equal(gp[:, 0], rp[:, 0])
-    # radii ~10 here: a few ulp of the coordinate
-    np.testing.assert_allclose(gp, rp, rtol=TOL_TRIG_REL, atol=0)
+    # radii ~10 here: a few ulp of the radius (y = axis + r cos(theta))
+    np.testing.assert_allclose(gp, rp, rtol=0, atol=TOL_TRIG_REL * pipe.to_numpy()[:, 3].max())
     np.testing.assert_array_equal(_np(vel), rv)
     table = pipe.to_numpy()
     for k in range(0, n, 997):
