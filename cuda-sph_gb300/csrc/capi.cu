@@ -464,9 +464,6 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     else if (c->density_variant == SPHGB_DENSITY_ROWS)
         SPHGB_CUDA(launch_density_rows(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
                                        c->tasks, c->big_count + 1));
-    else if (c->density_variant == SPHGB_DENSITY_TILED)
-        SPHGB_CUDA(launch_density_tiled(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
-                                        c->tasks, c->big_count + 1));
     else
         SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
@@ -651,7 +648,7 @@ int sphgb_ctx_set_tuning(SphgbCtx* ctx, int sort_block, int density_variant, int
         return fail(SPHGB_ERR_INVALID, "sort_block must be 128, 256 or 512");
     if (density_variant < SPHGB_DENSITY_WARP || density_variant > SPHGB_DENSITY_ROWS)
         return fail(SPHGB_ERR_INVALID,
-                    "density_variant must be SPHGB_DENSITY_WARP, _THREAD, _TILED or _ROWS");
+                    "density_variant must be SPHGB_DENSITY_WARP, _THREAD or _ROWS");
     if (big_voxel < kMinBigVoxel || big_voxel > 4096)
         return fail(SPHGB_ERR_INVALID, "big_voxel must be in [16, 4096]");
     ctx->sort_block = sort_block;

@@ -381,7 +381,7 @@ struct Launch {
 // kRowX voxels along x, or (overflow voxel, ~scene) for a scene's overflow bucket
 constexpr int kTaskRuns = 0;
 constexpr int kTaskRows = 1;
-constexpr int kRowX = 16;
+constexpr int kRowX = 20;
 
 // cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow bucket
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
@@ -418,10 +418,6 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t*
 cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_t* vstart,
                                 const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
                                 const int2* tasks, const int32_t* task_count);
-// the same with 8 lanes per particle and 8 candidates per lane
-cudaError_t launch_density_tiled(const Launch& L, const float4* pos, const int32_t* vstart,
-                                 const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                                 const int2* tasks, const int32_t* task_count);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float2* aux, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);

@@ -313,7 +313,7 @@ __device__ __noinline__ void density_one_call(int s, const SceneDev& sc,
 }
 
 constexpr int kRowThreads = 256;
-constexpr int kRowStage = 2560;                 // staged particles (40 KB)
+constexpr int kRowStage = 2816;                 // staged particles (44 KB)
 constexpr int kRowSpan = kRowX + 2;             // x0 - 1 .. x0 + kRowX
 
 struct RowShared {
@@ -415,43 +415,48 @@ k_density_rows(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ 
                 const float gx0 = fx * fx, gx2 = (vs0 - fx) * (vs0 - fx);
                 const float gy0 = fy * fy, gy2 = (vs1 - fy) * (vs1 - fy);
                 const float gz0 = fz * fz, gz2 = (vs2 - fz) * (vs2 - fz);
-                int na = 0;
-#pragma unroll 1
-                for (int ddx = 0; ddx < 3; ++ddx) {
+                // bit v: walk voxel v (walk() order) is in the table, not culled
+                // and not empty
+                unsigned vmask = 0;
+#pragma unroll
+                for (int v = 0; v < 27; ++v) {
+                    const int ddx = v / 9, ddy = (v / 3) % 3, ddz = v % 3;
                     const int nx = cx + ddx - 1;
-                    if (nx < 0 || nx >= D0) continue;
-                    const int xo = nx - x0 + 1;
-                    const float gx = ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f);
-#pragma unroll 1
-                    for (int ddy = 0; ddy < 3; ++ddy) {
-                        const float gxy = gx + (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
-#pragma unroll 1
-                        for (int ddz = 0; ddz < 3; ++ddz) {
-                            if (gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > cull2) continue;
-                            const int k = ddy * 3 + ddz;
-                            const int c = S.vc[k][xo];
-                            const int j0 = S.vs[k][xo];
-                            const float4* sp = S.pos + S.base[k];
-#pragma unroll 2
-                            for (int m = 0; m < c; ++m) {
-                                const int j = j0 + m;
-                                const float4 pj = sp[j];
-                                float dx, dy, dz, d2;
-                                if (within(pi, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2)) {
-                                    if (j != s) {
-                                        // d2 is the density sum's own distance arithmetic
-                                        const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-                                        acc.add(u * u * u);
-                                        if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
-                                        ++others;
-                                    }
-                                    if (++na >= cap) goto walked;
-                                }
-                            }
-                        }
-                    }
+                    const float gxy = (ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f)) +
+                                      (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
+                    const float g = gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f));
+                    if (nx >= 0 && nx < D0 && !(g > cull2) && S.vc[ddy * 3 + ddz][nx - x0 + 1] > 0)
+                        vmask |= 1u << v;
                 }
-            walked:;
+                // one flat loop over the candidates of those voxels in walk
+                // order, so that the lanes of a warp stay together
+                int na = 0, j = 0, jend = 0;
+                const float4* sp = S.pos;
+                for (;;) {
+                    if (j >= jend) {
+                        if (!vmask) break;
+                        const int v = __ffs(vmask) - 1;
+                        vmask &= vmask - 1;
+                        const int ddx = v / 9, k = v - 9 * ddx;
+                        const int xo = cx + ddx - x0;
+                        j = S.vs[k][xo];
+                        jend = j + S.vc[k][xo];
+                        sp = S.pos + S.base[k];
+                    }
+                    const float4 pj = sp[j];
+                    float dx, dy, dz, d2;
+                    if (within(pi, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2)) {
+                        if (j != s) {
+                            // d2 is the density sum's own distance arithmetic
+                            const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                            acc.add(u * u * u);
+                            if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
+                            ++others;
+                        }
+                        if (++na >= cap) break;
+                    }
+                    ++j;
+                }
             }
             const float r = (acc.s * sc.w_const) * sc.mass;
             rho[s] = r;
@@ -461,204 +466,6 @@ k_density_rows(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ 
             }
             if (nbr.count) nbr.count[s] = others;
         }
-    }
-}
-
-// Tiled density pass: one warp per task as above, but the warp is split into
-// four 8-lane segments, each serving one home particle, and each lane tests 8
-// consecutive candidates of the walk per batch (64 per home per batch).  The
-// walk's candidates are staged chunk by chunk in shared memory (coordinates as
-// separate x, y, z arrays, read as packed FP32 pairs).  A lane's accepted
-// candidates form an 8-bit mask; an exclusive scan of the mask counts over the
-// segment ranks them in walk order (lanes in order, then slots in order), so
-// again exactly the first MAX_NEIGHBOURS (self included) are kept, with the
-// same distance arithmetic and FP64 guard-band decision as k_density_wc: the
-// results are bit-identical to it.
-constexpr int kTlWarps = 4;
-constexpr int kTlChunk = 256;                        // candidates staged per chunk
-constexpr int kTlPadded = kTlChunk + 2 * (kTlChunk / 16);
-
-// two floats of padding every 16: 8-byte aligned pairs, and the 8 lanes of a
-// segment (8 candidates apart) hit distinct banks
-__device__ __forceinline__ int tl_index(int t) { return t + 2 * (t >> 4); }
-
-struct TlShared {
-    float cx[kTlPadded], cy[kTlPadded], cz[kTlPadded];
-    int32_t slot[kTlChunk];
-    float4 home[32];
-    int32_t list[32][kWcList + 1];
-    int32_t cnt[32];    // accepted candidates of each home particle so far (uncapped)
-    int32_t P[28];
-    int32_t st[27];
-};
-
-__global__ void __launch_bounds__(kTlWarps * 32)
-k_density_tiled(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
-                int n_scenes, int n, const float4* __restrict__ pos,
-                const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
-                float* __restrict__ rho, float2* __restrict__ aux, NbrList nbr,
-                const int2* __restrict__ tasks, const int32_t* __restrict__ task_count) {
-    __shared__ TlShared sh[kTlWarps];
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int seg = lane >> 3, j = lane & 7;
-    TlShared& S = sh[threadIdx.x >> 5];
-    const float inf = __int_as_float(0x7f800000);
-    const int n_tasks = *task_count;
-    for (int t = blockIdx.x * kTlWarps + (threadIdx.x >> 5); t < n_tasks;
-         t += gridDim.x * kTlWarps) {
-        const int2 task = tasks[t];
-        const int vid = task.x, d0 = task.y;
-        const SceneDev& sc = scenes[scene_of(d0, pbegin, n_scenes)];
-        const int vst = __ldg(vstart + vid), vc = __ldg(vcount + vid);
-        const int c_t = min(32, vst + vc - d0);
-        const int s = d0 + lane;
-        const bool home = lane < c_t;
-        const float4 pi = home ? __ldg(pos + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const int local = vid - sc.v_begin;
-        const int cap = sc.cap;
-        if (local == sc.v_count || cap > kListCap) {
-            if (home) density_one(s, pi, sc, pos, vstart, vcount, n, rho, aux, nbr, &S.list[lane][0], 1);
-            __syncwarp();
-            continue;
-        }
-        S.home[lane] = pi;
-        S.cnt[lane] = 0;
-        int ck = 0, stk = 0;
-        if (lane < 27) {
-            const int D0 = sc.dims[0], D1 = sc.dims[1];
-            const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
-            const int vx = local % D0, vy = (local / D0) % D1, vz = local / (D0 * D1);
-            const int nx = vx + lane / 9 - 1, ny = vy + (lane / 3) % 3 - 1, nz = vz + lane % 3 - 1;
-            if (nx >= 0 && nx < w0 && ny >= 0 && ny < w1 && nz >= 0 && nz < w2) {
-                const int id = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
-                ck = __ldg(vcount + id);
-                stk = __ldg(vstart + id);
-            }
-        }
-        int incl = ck;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(full, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane < 27) { S.P[lane] = incl - ck; S.st[lane] = stk; }
-        const int M = __shfl_sync(full, incl, 26);
-        __syncwarp();
-        const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
-        const double h_d = sc.h_d;
-        const int n_groups = (c_t + 3) >> 2;
-        for (int c0 = 0; c0 < M; c0 += kTlChunk) {
-            if (!__any_sync(full, home && S.cnt[lane] < cap)) break;
-            const int cm = min(kTlChunk, M - c0);
-            // stage the chunk; slots past its end hold +inf (never within h)
-            for (int u = lane; u < kTlChunk; u += 32) {
-                float x = inf, y = inf, z = inf;
-                int sl = -1;
-                if (u < cm) {
-                    const int q = c0 + u;
-                    int lo = 0, hi = 26;            // last walk voxel with P <= q
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (S.P[mid] <= q) lo = mid; else hi = mid - 1;
-                    }
-                    sl = S.st[lo] + (q - S.P[lo]);
-                    const float4 p = __ldg(pos + sl);
-                    x = p.x; y = p.y; z = p.z;
-                }
-                const int ui = tl_index(u);
-                S.cx[ui] = x; S.cy[ui] = y; S.cz[ui] = z;
-                S.slot[u] = sl;
-            }
-            __syncwarp();
-            for (int g = 0; g < n_groups; ++g) {
-                const int h = 4 * g + seg;
-                const bool act = h < c_t;
-                int hc = act ? S.cnt[h] : cap;      // same in the 8 lanes of a segment
-                const float4 ph = S.home[act ? h : 0];
-                const f32x2 hx = f2pack(ph.x, ph.x), hy = f2pack(ph.y, ph.y), hz = f2pack(ph.z, ph.z);
-                for (int b0 = 0; b0 < cm; b0 += 64) {
-                    if (!__any_sync(full, hc < cap)) break;
-                    const int qb = b0 + 8 * j;      // this lane's 8 candidates: qb .. qb + 7
-                    unsigned m = 0, near = 0;
-#pragma unroll
-                    for (int p = 0; p < 4; ++p) {
-                        const int ui = tl_index(qb + 2 * p);
-                        const f32x2 cx = *reinterpret_cast<const f32x2*>(&S.cx[ui]);
-                        const f32x2 cy = *reinterpret_cast<const f32x2*>(&S.cy[ui]);
-                        const f32x2 cz = *reinterpret_cast<const f32x2*>(&S.cz[ui]);
-                        const f32x2 dx = f2sub(hx, cx), dy = f2sub(hy, cy), dz = f2sub(hz, cz);
-                        f32x2 d2p = f2mul(dx, dx);
-                        d2p = f2fma(dy, dy, d2p);
-                        d2p = f2fma(dz, dz, d2p);
-                        float d20, d21;
-                        f2unpack(d2p, d20, d21);
-                        m |= ((unsigned)(d20 < h2_lo) << (2 * p)) | ((unsigned)(d21 < h2_lo) << (2 * p + 1));
-                        near |= ((unsigned)(d20 <= h2_hi) << (2 * p)) |
-                                ((unsigned)(d21 <= h2_hi) << (2 * p + 1));
-                    }
-                    if (hc >= cap) m = near = 0;    // capped or no home: nothing to record
-                    unsigned band = near & ~m;
-                    if (__any_sync(full, band != 0)) {
-                        while (band) {
-                            const int k = __ffs(band) - 1;
-                            band &= band - 1;
-                            const int ui = tl_index(qb + k);
-                            if (within_exact(ph.x, ph.y, ph.z, S.cx[ui], S.cy[ui], S.cz[ui], h_d))
-                                m |= 1u << k;
-                        }
-                    }
-                    const int c = __popc(m);
-                    int inc = c;
-#pragma unroll
-                    for (int o = 1; o < 8; o <<= 1) {
-                        const int v = __shfl_up_sync(full, inc, o, 8);
-                        if (j >= o) inc += v;
-                    }
-                    const int tot = __shfl_sync(full, inc, 7, 8);
-                    int r = hc + inc - c;
-                    while (m && r < cap) {
-                        const int k = __ffs(m) - 1;
-                        m &= m - 1;
-                        S.list[h][r] = S.slot[qb + k];
-                        ++r;
-                    }
-                    hc += tot;
-                }
-                if (act && j == 0) S.cnt[h] = hc;
-                __syncwarp();
-            }
-        }
-        __syncwarp();
-        if (home) {
-            const int na = min(S.cnt[lane], cap);
-            const float inv_h2 = 1.0f / sc.h2;
-            Kahan acc;
-            int others = 0;
-            for (int k = 0; k < na; ++k) {
-                const int jj = S.list[lane][k];
-                if (jj == s) continue;
-                const float4 pj = __ldg(pos + jj);
-                const float dx = __fsub_rn(pi.x, pj.x);
-                const float dy = __fsub_rn(pi.y, pj.y);
-                const float dz = __fsub_rn(pi.z, pj.z);
-                float d2 = __fmul_rn(dx, dx);
-                d2 = __fmaf_rn(dy, dy, d2);
-                d2 = __fmaf_rn(dz, dz, d2);
-                const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-                acc.add(u * u * u);
-                if (nbr.idx) nbr.idx[(size_t)others * n + s] = jj;
-                ++others;
-            }
-            const float r = (acc.s * sc.w_const) * sc.mass;
-            rho[s] = r;
-            if (aux) {
-                const float p = sc.k * (r - sc.rho0);
-                aux[s] = make_float2(p / (r * r), 1.0f / r);
-            }
-            if (nbr.count) nbr.count[s] = others;
-        }
-        __syncwarp();
     }
 }
 
@@ -959,20 +766,6 @@ cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_
     k_density_rows<<<blocks, kRowThreads, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                           vstart, vcount, rho, aux, nbr, tasks,
                                                           task_count);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_density_tiled(const Launch& L, const float4* pos, const int32_t* vstart,
-                                 const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                                 const int2* tasks, const int32_t* task_count) {
-    if (L.n == 0) return cudaSuccess;
-    // persistent grid: 5 blocks of 4 warps per SM (82 registers per thread,
-    // 38 KB shared per block), warps stride over the tasks
-    int blocks = (L.n + 32 * kTlWarps - 1) / (32 * kTlWarps);
-    if (blocks > 152 * 5) blocks = 152 * 5;
-    k_density_tiled<<<blocks, kTlWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n,
-                                                            pos, vstart, vcount, rho, aux, nbr,
-                                                            tasks, task_count);
     return cudaGetLastError();
 }
 

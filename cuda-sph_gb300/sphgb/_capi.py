@@ -13,7 +13,7 @@ from . import _build
 
 MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
-DENSITY_WARP, DENSITY_THREAD, DENSITY_TILED, DENSITY_ROWS = 0, 1, 2, 3
+DENSITY_WARP, DENSITY_THREAD, DENSITY_ROWS = 0, 1, 2
 
 ERRORS = {
     -1: "SPHGB_ERR_INVALID",
