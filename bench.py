@@ -73,7 +73,7 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched/served sections")
     ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--batched-steps", type=int, default=50)
-    ap.add_argument("--tuning", choices=["auto", "default", "warp", "rows", "thread"],
+    ap.add_argument("--tuning", choices=["auto", "default", "warp", "thread"],
                     default="auto", help="launch tuning: autotuned on the scene, the library "
                     "defaults, or the defaults with the named density kernel")
     ap.add_argument("--served-requests", type=int, default=24)
@@ -244,7 +244,7 @@ def run_gb300(args):
     else:
         best, tried = Tuning(), []
         if args.tuning != "default":
-            best.density_variant = {"warp": 0, "thread": 1, "rows": 2}[args.tuning]
+            best.density_variant = {"warp": 0, "thread": 1}[args.tuning]
     log(f"tuning: {best}")
     batch = SceneBatch([spec], device=str(dev))
     best.apply(batch)
@@ -339,7 +339,7 @@ def run_gb300(args):
                       "input": "every step is a full step of the same resident step-0 state"},
            "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
            "free_running": free,
-           "autotune": {"chosen": {"density": {0: "warp", 1: "thread", 2: "rows"}[best.density_variant],
+           "autotune": {"chosen": {"density": {0: "warp", 1: "thread"}[best.density_variant],
                                    "sort_block": best.sort_block, "big_voxel": best.big_voxel},
                         "ms_per_step": summary(tried)},
            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}

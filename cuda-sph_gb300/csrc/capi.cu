@@ -130,7 +130,6 @@ struct SphgbCtx {
         L.pipe_scenes = any_pipe;
         L.sort_block = sort_block;
         L.big_voxel = big_voxel;
-        L.task_kind = density_variant == SPHGB_DENSITY_ROWS ? kTaskRows : kTaskRuns;
         L.stream = st;
         return L;
     }
@@ -461,9 +460,6 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     if (c->density_variant == SPHGB_DENSITY_WARP)
         SPHGB_CUDA(launch_density_wc(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
                                      c->tasks, c->big_count + 1));
-    else if (c->density_variant == SPHGB_DENSITY_ROWS)
-        SPHGB_CUDA(launch_density_rows(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
-                                       c->tasks, c->big_count + 1));
     else
         SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
@@ -646,9 +642,8 @@ int sphgb_ctx_set_tuning(SphgbCtx* ctx, int sort_block, int density_variant, int
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (sort_block != 128 && sort_block != 256 && sort_block != 512)
         return fail(SPHGB_ERR_INVALID, "sort_block must be 128, 256 or 512");
-    if (density_variant < SPHGB_DENSITY_WARP || density_variant > SPHGB_DENSITY_ROWS)
-        return fail(SPHGB_ERR_INVALID,
-                    "density_variant must be SPHGB_DENSITY_WARP, _THREAD or _ROWS");
+    if (density_variant != SPHGB_DENSITY_WARP && density_variant != SPHGB_DENSITY_THREAD)
+        return fail(SPHGB_ERR_INVALID, "density_variant must be SPHGB_DENSITY_WARP or _THREAD");
     if (big_voxel < kMinBigVoxel || big_voxel > 4096)
         return fail(SPHGB_ERR_INVALID, "big_voxel must be in [16, 4096]");
     ctx->sort_block = sort_block;

@@ -238,8 +238,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
               float4* __restrict__ pos_out, float4* __restrict__ vel_out,
               int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
               int2* __restrict__ tasks, int32_t* __restrict__ task_count, int big_voxel,
-              const int32_t* __restrict__ slot, const SceneDev* __restrict__ scenes,
-              const int32_t* __restrict__ pbegin, int n_scenes, int task_kind) {
+              const int32_t* __restrict__ slot) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int code = cell[s];
@@ -261,23 +260,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
         r = lo;
     }
     const int d = st + r;
-    if (tasks) {
-        if (task_kind == kTaskRuns) {
-            if ((r & 31) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
-        } else if (r == 0) {
-            const int si = scene_of(s, pbegin, n_scenes);
-            if (code < 0) {
-                tasks[atomicAdd(task_count, 1)] = make_int2(vid, ~si);
-            } else {
-                // the first occupied voxel of its chunk emits the chunk: no
-                // member before it in the chunk (equal starts)
-                const SceneDev& sc = scenes[si];
-                const int x = (vid - sc.v_begin) % sc.dims[0];
-                const int v0 = vid - x % kRowX;
-                if (__ldg(vstart + v0) == st) tasks[atomicAdd(task_count, 1)] = make_int2(v0, si);
-            }
-        }
-    }
+    if (tasks && (r & 31) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
     pid_out[d] = p;
     pos_out[d] = __ldg(pos + s);
     vel_out[d] = __ldg(vel + s);
@@ -341,8 +324,7 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
     k_rank_gather<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart, vcount,
                                                          pos, vel, pos64, pos_out, vel_out,
                                                          pid_out, pos64_out, tasks, task_count,
-                                                         L.big_voxel, slot, L.scenes, L.pbegin,
-                                                         L.n_scenes, L.task_kind);
+                                                         L.big_voxel, slot);
     return cudaGetLastError();
 }
 

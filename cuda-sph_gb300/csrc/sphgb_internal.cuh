@@ -354,7 +354,8 @@ __device__ inline void pipe_collide(double* p, double* v, const PipeView& P, uin
 
 // ---- neighbour list --------------------------------------------------------
 // Neighbours (other than self) of every particle in walk order, recorded by
-// the density pass and read by the force pass.  Column-major: idx[k * n + s].
+// the density pass and read by the force pass.  One row per particle:
+// idx[s * kListCap + k].
 constexpr int kListCap = 32;
 struct NbrList {
     int32_t* idx = nullptr;     // kListCap * n entries
@@ -372,16 +373,8 @@ struct Launch {
     bool pipe_scenes;           // some scene is in pipe mode
     int sort_block = kBlock;    // threads per block of the per-particle sort kernels
     int big_voxel = 64;         // voxels above this many members are sorted per block
-    int task_kind = 0;          // density tasks the rank-gather emits (kTask*)
     cudaStream_t stream;
 };
-
-// density tasks: kTaskRuns = (voxel, first slot) per run of <= 32 slots of a
-// voxel; kTaskRows = (first voxel of a row chunk, scene) per occupied chunk of
-// kRowX voxels along x, or (overflow voxel, ~scene) for a scene's overflow bucket
-constexpr int kTaskRuns = 0;
-constexpr int kTaskRows = 1;
-constexpr int kRowX = 20;
 
 // cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow bucket
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
@@ -413,11 +406,6 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vs
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
                               const int2* tasks, const int32_t* task_count);
-// one block per row chunk: the chunk's 27-voxel neighbourhood staged in shared
-// memory, one thread per particle
-cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_t* vstart,
-                                const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                                const int2* tasks, const int32_t* task_count);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float2* aux, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);

@@ -19,9 +19,9 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // Also writes aux_i = (p_i / rho_i^2, 1 / rho_i) with p = K (rho - RHO_0), the
 // per-particle factors of the force pass (voxel_kernels.py:162-164, :205-208),
 // and, when nbr is given, the particle's neighbours other than itself in walk
-// order (the set every later kernel of the step uses), column-major
-// nbr.idx[k * n + s]; nbr.count[s] = their number, or -1 when more than
-// kListCap (the force pass then walks again).
+// order (the set every later kernel of the step uses), one row per particle,
+// nbr.idx[s * kListCap + k]; nbr.count[s] = their number, or -1 when more
+// than kListCap (the force pass then walks again).
 // One particle's density by a thread-private walk: the walk records neighbour
 // slots in row[k * stride] (k < kListCap), the sum runs afterwards in walk
 // order; with more neighbours than that the walk is repeated, summing.
@@ -55,7 +55,7 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
             acc.add(u * u * u);
         }
         if (nbr.idx)
-            for (int k = 0; k < others; ++k) nbr.idx[(size_t)k * n + s] = row[k * stride];
+            for (int k = 0; k < others; ++k) nbr.idx[(size_t)s * kListCap + k] = row[k * stride];
     } else {
         // more neighbours than the list holds (no cap or a cap above it):
         // walk again, summing on the way
@@ -127,6 +127,9 @@ __device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
 // walk order with the same arithmetic as density_one: the results are
 // bit-identical to the thread-per-particle kernel.
 constexpr int kWcWarps = 8;
+// list entry of the particle itself once entries hold density terms: a NaN
+// bit pattern, which no term (a cube of a finite number) takes
+constexpr int kSelfTerm = 0x7fc0dead;
 constexpr int kWcList = kListCap;       // accepted neighbours per particle, self included
 
 struct WcShared {
@@ -204,7 +207,9 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         for (int b0 = 0; b0 < M; b0 += 64) {
             const int q0 = b0 + lane, q1 = q0 + 32;
             const bool v0 = q0 < M, v1 = q1 < M;
-            float4 pj0 = make_float4(0.f, 0.f, 0.f, 0.f), pj1 = pj0;
+            // past the end of the walk: +inf coordinates, never within h
+            const float inf = __int_as_float(0x7f800000);
+            float4 pj0 = make_float4(inf, inf, inf, 0.f), pj1 = pj0;
             int sj0 = -1, sj1 = -1;
             if (v0) {
                 int lo = 0, hi = 26;            // last walk voxel with P <= q
@@ -240,9 +245,8 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                 d2p = f2fma(dz, dz, d2p);
                 float d20, d21;
                 f2unpack(d2p, d20, d21);
-                bool acc0 = v0 && d20 < h2_lo, acc1 = v1 && d21 < h2_lo;
-                const bool band0 = v0 && d20 >= h2_lo && d20 <= h2_hi;
-                const bool band1 = v1 && d21 >= h2_lo && d21 <= h2_hi;
+                bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
+                const bool band0 = !acc0 && d20 <= h2_hi, band1 = !acc1 && d21 <= h2_hi;
                 if (__any_sync(full, band0 || band1)) {
                     const float4 ph = S.home[i];
                     if (band0) acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
@@ -257,24 +261,45 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             }
         }
         __syncwarp();
+        // (a) one lane per list entry: the density term of every accepted pair
+        // replaces the entry (self gets kSelfTerm), and each particle's list
+        // row (neighbours other than itself, walk order) is written coalesced
+        const float inv_h2 = 1.0f / sc.h2;
+        for (int i = 0; i < c_t; ++i) {
+            const int na_i = min(__shfl_sync(full, cnt, i), cap);
+            const int si = d0 + i;
+            const bool in = lane < na_i;
+            const int j = in ? S.list[i][lane] : -1;
+            const unsigned self = __ballot_sync(full, in && j == si);
+            if (in) {
+                int term = kSelfTerm;
+                if (j != si) {
+                    const float4 ph = S.home[i];
+                    const float4 pj = __ldg(pos + j);
+                    const float dx = __fsub_rn(ph.x, pj.x);
+                    const float dy = __fsub_rn(ph.y, pj.y);
+                    const float dz = __fsub_rn(ph.z, pj.z);
+                    float d2 = __fmul_rn(dx, dx);
+                    d2 = __fmaf_rn(dy, dy, d2);
+                    d2 = __fmaf_rn(dz, dz, d2);
+                    const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                    term = __float_as_int(u * u * u);
+                    if (nbr.idx) nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
+                }
+                S.list[i][lane] = term;
+            }
+        }
+        __syncwarp();
+        // (b) one lane per particle: the compensated sum in walk order, the
+        // arithmetic of density_one
         if (home) {
             const int na = min(cnt, cap);
-            const float inv_h2 = 1.0f / sc.h2;
             Kahan acc;
             int others = 0;
             for (int k = 0; k < na; ++k) {
-                const int j = S.list[lane][k];
-                if (j == s) continue;
-                const float4 pj = __ldg(pos + j);
-                const float dx = __fsub_rn(pi.x, pj.x);
-                const float dy = __fsub_rn(pi.y, pj.y);
-                const float dz = __fsub_rn(pi.z, pj.z);
-                float d2 = __fmul_rn(dx, dx);
-                d2 = __fmaf_rn(dy, dy, d2);
-                d2 = __fmaf_rn(dz, dz, d2);
-                const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-                acc.add(u * u * u);
-                if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
+                const int term = S.list[lane][k];
+                if (term == kSelfTerm) continue;
+                acc.add(__int_as_float(term));
                 ++others;
             }
             const float r = (acc.s * sc.w_const) * sc.mass;
@@ -301,174 +326,6 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
 // list.  Results are bit-identical to density_one.  Scenes in truncated-walk
 // mode or with a cap beyond the list, neighbourhoods beyond the shared
 // buffer and overflow buckets take density_one (global memory walk).
-// density_one out of line: the fallback paths of the row kernel keep their
-// registers out of its fast path
-__device__ __noinline__ void density_one_call(int s, const SceneDev& sc,
-                                              const float4* __restrict__ pos,
-                                              const int32_t* __restrict__ vstart,
-                                              const int32_t* __restrict__ vcount, int n,
-                                              float* __restrict__ rho, float2* __restrict__ aux,
-                                              NbrList nbr, int32_t* row, int stride) {
-    density_one(s, __ldg(pos + s), sc, pos, vstart, vcount, n, rho, aux, nbr, row, stride);
-}
-
-constexpr int kRowThreads = 256;
-constexpr int kRowStage = 2816;                 // staged particles (44 KB)
-constexpr int kRowSpan = kRowX + 2;             // x0 - 1 .. x0 + kRowX
-
-struct RowShared {
-    float4 pos[kRowStage];
-    int32_t vs[9][kRowSpan];    // start slot of each walk voxel of the chunk
-    int32_t vc[9][kRowSpan];    // member count (0 outside the table)
-    int32_t len[9], slot0[9], base[9];
-    int32_t fallback;
-};
-
-__global__ void __launch_bounds__(kRowThreads, 4)
-k_density_rows(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
-               int n_scenes, int n, const float4* __restrict__ pos,
-               const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
-               float* __restrict__ rho, float2* __restrict__ aux, NbrList nbr,
-               const int2* __restrict__ tasks, const int32_t* __restrict__ task_count) {
-    __shared__ RowShared S;
-    // per-thread list scratch of density_one (kListCap rows of kRowThreads)
-    int32_t* scratch = reinterpret_cast<int32_t*>(S.pos) + threadIdx.x;
-    static_assert(kListCap * kRowThreads * 4 <= (int)sizeof(S.pos), "scratch fits the stage");
-    const int n_tasks = *task_count;
-    for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
-        const int2 task = tasks[t];
-        __syncthreads();                        // the previous task is done with S
-        if (task.y < 0) {                       // overflow bucket: non-finite particles
-            const SceneDev& sc = scenes[~task.y];
-            const int st = __ldg(vstart + task.x), c = __ldg(vcount + task.x);
-            for (int s = st + threadIdx.x; s < st + c; s += blockDim.x)
-                density_one_call(s, sc, pos, vstart, vcount, n, rho, aux, nbr, scratch, kRowThreads);
-            continue;
-        }
-        const SceneDev& sc = scenes[task.y];
-        const int D0 = sc.dims[0], D1 = sc.dims[1], D2 = sc.dims[2];
-        const int cv = task.x - sc.v_begin;
-        const int x0 = cv % D0, y = (cv / D0) % D1, z = cv / (D0 * D1);
-        const int x1 = min(x0 + kRowX, D0);     // chunk voxels x0 .. x1 - 1
-        const int S0 = __ldg(vstart + task.x);
-        const int S1 = __ldg(vstart + task.x + (x1 - 1 - x0)) + __ldg(vcount + task.x + (x1 - 1 - x0));
-        if (threadIdx.x < 9) {
-            const int k = threadIdx.x;
-            const int ny = y + k / 3 - 1, nz = z + k % 3 - 1;
-            int len = 0, s0 = 0;
-            if (ny >= 0 && ny < D1 && nz >= 0 && nz < D2) {
-                const int row = sc.v_begin + ny * D0 + nz * D0 * D1;
-                const int xa = max(x0 - 1, 0), xb = min(x1, D0 - 1);
-                s0 = __ldg(vstart + row + xa);
-                len = __ldg(vstart + row + xb) + __ldg(vcount + row + xb) - s0;
-            }
-            S.len[k] = len;
-            S.slot0[k] = s0;
-        }
-        for (int i = threadIdx.x; i < 9 * kRowSpan; i += blockDim.x) {
-            const int k = i / kRowSpan, xo = i % kRowSpan;
-            const int nx = x0 - 1 + xo, ny = y + k / 3 - 1, nz = z + k % 3 - 1;
-            int vs = 0, vc = 0;
-            if (nx >= 0 && nx < D0 && ny >= 0 && ny < D1 && nz >= 0 && nz < D2) {
-                const int vid = sc.v_begin + nx + ny * D0 + nz * D0 * D1;
-                vs = __ldg(vstart + vid);
-                vc = __ldg(vcount + vid);
-            }
-            S.vs[k][xo] = vs;
-            S.vc[k][xo] = vc;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int off = 0;
-            for (int k = 0; k < 9; ++k) {
-                S.base[k] = off - S.slot0[k];
-                off += S.len[k];
-            }
-            S.fallback = off > kRowStage || sc.walk_trunc || sc.cap > kListCap;
-        }
-        __syncthreads();
-        if (S.fallback) {
-            for (int s = S0 + threadIdx.x; s < S1; s += blockDim.x)
-                density_one_call(s, sc, pos, vstart, vcount, n, rho, aux, nbr, scratch, kRowThreads);
-            continue;
-        }
-        for (int k = 0; k < 9; ++k) {
-            const int len = S.len[k], s0 = S.slot0[k], b = S.base[k] + s0;
-            for (int i = threadIdx.x; i < len; i += blockDim.x) S.pos[b + i] = __ldg(pos + s0 + i);
-        }
-        __syncthreads();
-        const float vs0 = sc.vs[0], vs1 = sc.vs[1], vs2 = sc.vs[2];
-        const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi, cull2 = sc.cull2;
-        const double h_d = sc.h_d;
-        const int cap = sc.cap;
-        const float inv_h2 = 1.0f / sc.h2;
-        for (int s = S0 + threadIdx.x; s < S1; s += blockDim.x) {
-            const float4 pi = S.pos[S.base[4] + s];
-            Kahan acc;
-            int others = 0;
-            if (finite3(pi)) {
-                const int cx = voxel_coord(pi.x, vs0, D0);
-                // squared distances to the own voxel's faces (the culling of walk())
-                const float fx = pi.x - (float)cx * vs0;
-                const float fy = pi.y - (float)y * vs1;
-                const float fz = pi.z - (float)z * vs2;
-                const float gx0 = fx * fx, gx2 = (vs0 - fx) * (vs0 - fx);
-                const float gy0 = fy * fy, gy2 = (vs1 - fy) * (vs1 - fy);
-                const float gz0 = fz * fz, gz2 = (vs2 - fz) * (vs2 - fz);
-                // bit v: walk voxel v (walk() order) is in the table, not culled
-                // and not empty
-                unsigned vmask = 0;
-#pragma unroll
-                for (int v = 0; v < 27; ++v) {
-                    const int ddx = v / 9, ddy = (v / 3) % 3, ddz = v % 3;
-                    const int nx = cx + ddx - 1;
-                    const float gxy = (ddx == 0 ? gx0 : (ddx == 2 ? gx2 : 0.0f)) +
-                                      (ddy == 0 ? gy0 : (ddy == 2 ? gy2 : 0.0f));
-                    const float g = gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f));
-                    if (nx >= 0 && nx < D0 && !(g > cull2) && S.vc[ddy * 3 + ddz][nx - x0 + 1] > 0)
-                        vmask |= 1u << v;
-                }
-                // one flat loop over the candidates of those voxels in walk
-                // order, so that the lanes of a warp stay together
-                int na = 0, j = 0, jend = 0;
-                const float4* sp = S.pos;
-                for (;;) {
-                    if (j >= jend) {
-                        if (!vmask) break;
-                        const int v = __ffs(vmask) - 1;
-                        vmask &= vmask - 1;
-                        const int ddx = v / 9, k = v - 9 * ddx;
-                        const int xo = cx + ddx - x0;
-                        j = S.vs[k][xo];
-                        jend = j + S.vc[k][xo];
-                        sp = S.pos + S.base[k];
-                    }
-                    const float4 pj = sp[j];
-                    float dx, dy, dz, d2;
-                    if (within(pi, pj, h2_lo, h2_hi, h_d, dx, dy, dz, d2)) {
-                        if (j != s) {
-                            // d2 is the density sum's own distance arithmetic
-                            const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-                            acc.add(u * u * u);
-                            if (nbr.idx) nbr.idx[(size_t)others * n + s] = j;
-                            ++others;
-                        }
-                        if (++na >= cap) break;
-                    }
-                    ++j;
-                }
-            }
-            const float r = (acc.s * sc.w_const) * sc.mass;
-            rho[s] = r;
-            if (aux) {
-                const float p = sc.k * (r - sc.rho0);
-                aux[s] = make_float2(p / (r * r), 1.0f / r);
-            }
-            if (nbr.count) nbr.count[s] = others;
-        }
-    }
-}
-
 __global__ void __launch_bounds__(kBlock)
 k_aux(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
       int n, const float* __restrict__ rho, float2* __restrict__ aux) {
@@ -561,17 +418,23 @@ __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& 
                                                 ForceSums<kPlain>& f) {
     const float inv_h = 1.0f / sc.h;
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
-#pragma unroll 4
-    for (int k = 0; k < cnt; ++k) {
-        const int j = __ldg(list + (size_t)k * n);
-        const float4 pj = __ldg(pos + j);
-        const float dx = __fsub_rn(pi.x, pj.x);
-        const float dy = __fsub_rn(pi.y, pj.y);
-        const float dz = __fsub_rn(pi.z, pj.z);
-        float d2 = __fmul_rn(dx, dx);
-        d2 = __fmaf_rn(dy, dy, d2);
-        d2 = __fmaf_rn(dz, dz, d2);
-        add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
+    // the row is 16-byte aligned: four entries per load
+    for (int k0 = 0; k0 < cnt; k0 += 4) {
+        const int4 q = __ldg(reinterpret_cast<const int4*>(list) + (k0 >> 2));
+        const int js[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k0 + u >= cnt) break;
+            const int j = js[u];
+            const float4 pj = __ldg(pos + j);
+            const float dx = __fsub_rn(pi.x, pj.x);
+            const float dy = __fsub_rn(pi.y, pj.y);
+            const float dz = __fsub_rn(pi.z, pj.z);
+            float d2 = __fmul_rn(dx, dx);
+            d2 = __fmaf_rn(dy, dy, d2);
+            d2 = __fmaf_rn(dz, dz, d2);
+            add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
+        }
     }
 }
 
@@ -662,7 +525,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const float rho_i = __ldg(rho + s);
     const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
     const Forces f = forces_of(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount,
-                               nbr.idx ? nbr.idx + s : nullptr, n, cnt);
+                               nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr, n, cnt);
     const float vscale = sc.mass * sc.visc * ai.y;
     // result_force = ext + -P + V (base_kernels.py:46-52)
     float F[3];
@@ -753,19 +616,6 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t*
     k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                          vstart, vcount, rho, aux, nbr, tasks,
                                                          task_count);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_density_rows(const Launch& L, const float4* pos, const int32_t* vstart,
-                                const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                                const int2* tasks, const int32_t* task_count) {
-    if (L.n == 0) return cudaSuccess;
-    // persistent grid: 4 blocks of 256 threads per SM, blocks stride over the chunks
-    int blocks = (L.n + 127) / 128;
-    if (blocks > 152 * 4) blocks = 152 * 4;
-    k_density_rows<<<blocks, kRowThreads, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                          vstart, vcount, rho, aux, nbr, tasks,
-                                                          task_count);
     return cudaGetLastError();
 }
 

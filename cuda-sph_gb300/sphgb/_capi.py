@@ -13,7 +13,7 @@ from . import _build
 
 MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
-DENSITY_WARP, DENSITY_THREAD, DENSITY_ROWS = 0, 1, 2
+DENSITY_WARP, DENSITY_THREAD = 0, 1
 
 ERRORS = {
     -1: "SPHGB_ERR_INVALID",

@@ -1,10 +1,8 @@
 """Autotuner for the launch choices of a batch of scenes.
 
 Tunes what changes speed but not results:
-* the density kernel variant: one warp per voxel run (SPHGB_DENSITY_WARP,
-  one lane per candidate), best when voxels hold few particles; one block per
-  chunk of a voxel-table row with the neighbourhood staged in shared memory
-  (SPHGB_DENSITY_ROWS); or one thread per particle with
+* the density kernel variant: one warp per voxel run (SPHGB_DENSITY_WARP),
+  best when voxels hold few particles, or one thread per particle with
   per-particle voxel culling and early exit (SPHGB_DENSITY_THREAD), best in
   dense scenes;
 * the block size of the per-particle sort kernels;
@@ -30,7 +28,7 @@ from . import _capi
 from .data_classes import SimulationState
 from .device import SceneBatch, SceneSpec
 
-VARIANTS = (_capi.DENSITY_WARP, _capi.DENSITY_ROWS, _capi.DENSITY_THREAD)
+VARIANTS = (_capi.DENSITY_WARP, _capi.DENSITY_THREAD)
 SORT_BLOCKS = (128, 256, 512)
 BIG_VOXEL = (32, 64, 256)
 CELL_RATIOS = (1.0, 1.25, 1.5)
@@ -83,7 +81,6 @@ def autotune(pairs: Sequence[Tuple[SceneSpec, SimulationState]], steps: int = 3,
 
 
 def summary(tried: List[Tuning]) -> Dict[str, float]:
-    names = {_capi.DENSITY_WARP: "warp", _capi.DENSITY_THREAD: "thread",
-             _capi.DENSITY_ROWS: "rows"}
+    names = {_capi.DENSITY_WARP: "warp", _capi.DENSITY_THREAD: "thread"}
     return {f"{names[t.density_variant]}/b{t.sort_block}/big{t.big_voxel}/r{t.cell_ratio}":
             round(t.ms_per_step, 4) for t in tried}

@@ -45,7 +45,7 @@ enum {
 enum { SPHGB_MODE_BOX = 0, SPHGB_MODE_PIPE = 1 };      /* config.SIM_MODE (config.py:13) */
 enum { SPHGB_WALK_CEIL = 0, SPHGB_WALK_TRUNCATED = 1 }; /* see walk_dims below */
 /* sphgb_ctx_set_tuning */
-enum { SPHGB_DENSITY_WARP = 0, SPHGB_DENSITY_THREAD = 1, SPHGB_DENSITY_ROWS = 2 };
+enum { SPHGB_DENSITY_WARP = 0, SPHGB_DENSITY_THREAD = 1 };
 
 /*
  * One scene: SimulationParameters (common/data_classes.py:70-78) plus the
@@ -111,9 +111,7 @@ int sphgb_ctx_reconfigure(SphgbCtx* ctx, const SphgbSceneParams* scenes, int n_s
 /* Launch tuning (results do not change): threads per block of the
  * per-particle sort kernels (128, 256, 512), the density kernel variant
  * (SPHGB_DENSITY_WARP: one warp per voxel run, one lane per candidate;
- * SPHGB_DENSITY_ROWS: one block per chunk of 20 voxels
- * of a table row, its neighbourhood staged in shared memory, one thread per
- * particle; SPHGB_DENSITY_THREAD: one thread per particle) and the member count above which a voxel is sorted by
+ * SPHGB_DENSITY_THREAD: one thread per particle) and the member count above which a voxel is sorted by
  * a block of its own (16..4096).  No counterpart in the reference (numba picks
  * one block size per device, thread_layout.py:27-33). */
 int sphgb_ctx_set_tuning(SphgbCtx* ctx, int sort_block, int density_variant, int big_voxel);

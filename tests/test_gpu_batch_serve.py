@@ -94,8 +94,7 @@ def test_reconfigure_and_tuning_keep_results():
     other, ost = scenes.pipe_flow(n=5000, seed=2, h=0.05)
     b = SceneBatch([other])
     b.reconfigure([spec])                  # smaller scratch needs: buffers reused
-    for tuning in ((128, _capi.DENSITY_THREAD, 16), (512, _capi.DENSITY_WARP, 256),
-                   (256, _capi.DENSITY_ROWS, 32)):
+    for tuning in ((128, _capi.DENSITY_THREAD, 16), (512, _capi.DENSITY_WARP, 256)):
         b.set_tuning(*tuning)
         b.load_states([st])
         b.step(3)

@@ -179,15 +179,15 @@ def test_conservation_sums_match_fp64_sums_of_the_state():
 
 @pytest.mark.parametrize("name", ["config0", "pipe", "uncapped", "truncated"])
 def test_density_variants_bit_identical(name):
-    """The three density kernels (lane per candidate, row chunks staged in
-    shared memory, thread per particle) keep the same neighbours in the same order and sum
+    """The two density kernels (warp per voxel run with a lane per
+    candidate, thread per particle) keep the same neighbours in the same order and sum
     them the same way: identical states after several steps."""
     torch_cuda()
     from sphgb import _capi
     from sphgb.device import SceneBatch
     spec, st = _scenes()[name]
     outs = []
-    for variant in (_capi.DENSITY_WARP, _capi.DENSITY_ROWS, _capi.DENSITY_THREAD):
+    for variant in (_capi.DENSITY_WARP, _capi.DENSITY_THREAD):
         b = SceneBatch([spec])
         b.set_tuning(256, variant, 64)
         b.load_states([st])
@@ -212,7 +212,7 @@ def test_density_variants_identical_on_dense_voxels():
              scenes.pipe_flow(n=30_000, seed=13, h=0.02)]
     for spec, st in cases:
         outs = []
-        for variant in (_capi.DENSITY_WARP, _capi.DENSITY_ROWS, _capi.DENSITY_THREAD):
+        for variant in (_capi.DENSITY_WARP, _capi.DENSITY_THREAD):
             b = SceneBatch([spec])
             b.set_tuning(256, variant, 64)
             b.load_states([st])
