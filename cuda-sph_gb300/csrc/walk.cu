@@ -75,17 +75,6 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
     if (nbr.count) nbr.count[s] = others <= kListCap ? others : -1;
 }
 
-// density_one out of line, for the rare fallback of the warp-cooperative
-// kernel (keeps its registers out of that kernel's common path)
-__device__ __noinline__ void density_one_call(int s, const SceneDev& sc,
-                                              const float4* __restrict__ pos,
-                                              const int32_t* __restrict__ vstart,
-                                              const int32_t* __restrict__ vcount, int n,
-                                              float* __restrict__ rho, float2* __restrict__ aux,
-                                              NbrList nbr, int32_t* row, int stride) {
-    density_one(s, __ldg(pos + s), sc, pos, vstart, vcount, n, rho, aux, nbr, row, stride);
-}
-
 // thread per particle (used by the stage entry points and as the reference
 // path of the warp-cooperative kernel below)
 __global__ void __launch_bounds__(kBlock)
@@ -152,7 +141,7 @@ struct WcShared {
     int32_t st[27];     // first slot of each walk voxel
 };
 
-__global__ void __launch_bounds__(kWcWarps * 32, 4)
+__global__ void __launch_bounds__(kWcWarps * 32)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
              int n_scenes, int n, const float4* __restrict__ pos,
              const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
@@ -179,7 +168,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home) density_one_call(s, sc, pos, vstart, vcount, n, rho, aux, nbr, &S.list[lane][0], 1);
+            if (home) density_one(s, pi, sc, pos, vstart, vcount, n, rho, aux, nbr, &S.list[lane][0], 1);
             __syncwarp();
             continue;
         }
@@ -457,16 +446,14 @@ struct Forces {
 // Kahan sums, redone plainly when a factor of particle i or of a neighbour
 // is non-finite (a particle of density 0).  With a neighbour list (cnt >= 0)
 // the neighbours come from it, else from a fresh walk.
-// The general case, out of line so that its registers stay out of the
-// common path of forces_of below.
-__device__ __noinline__ Forces forces_general(int s, const float4 pi, const float4 vi,
-                                              const float2 ai, const SceneDev& sc,
-                                              const float4* __restrict__ pos,
-                                              const float4* __restrict__ vel,
-                                              const float2* __restrict__ aux,
-                                              const int32_t* __restrict__ vstart,
-                                              const int32_t* __restrict__ vcount,
-                                              const int32_t* __restrict__ list, int n, int cnt) {
+__device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float4& vi,
+                                            const float2& ai, const SceneDev& sc,
+                                            const float4* __restrict__ pos,
+                                            const float4* __restrict__ vel,
+                                            const float2* __restrict__ aux,
+                                            const int32_t* __restrict__ vstart,
+                                            const int32_t* __restrict__ vcount,
+                                            const int32_t* __restrict__ list, int n, int cnt) {
     Forces out;
     bool plain = !(fabsf(ai.x * ai.y) < INFINITY);
     if (!plain) {
@@ -483,25 +470,6 @@ __device__ __noinline__ Forces forces_general(int s, const float4 pi, const floa
         out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
     }
     return out;
-}
-
-// Common path: finite factors and a recorded neighbour list, compensated
-// sums over the list; anything else (a fresh walk, a non-finite factor that
-// needs the plain sums) goes to forces_general, with the same results.
-__device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float4& vi,
-                                            const float2& ai, const SceneDev& sc,
-                                            const float4* __restrict__ pos,
-                                            const float4* __restrict__ vel,
-                                            const float2* __restrict__ aux,
-                                            const int32_t* __restrict__ vstart,
-                                            const int32_t* __restrict__ vcount,
-                                            const int32_t* __restrict__ list, int n, int cnt) {
-    if (cnt >= 0 && fabsf(ai.x * ai.y) < INFINITY) {
-        ForceSums<false> f;
-        force_sums_list<false>(pi, vi, ai.x, sc, pos, vel, aux, list, n, cnt, f);
-        if (!f.bad) return Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
-    }
-    return forces_general(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount, list, n, cnt);
 }
 
 __device__ __forceinline__ float clamp1(float x) { return x < 1.0f ? x : 1.0f; }  // min(1, x)
