@@ -77,7 +77,7 @@ struct SphgbCtx {
     float4* velB = nullptr;
     int32_t* pidB = nullptr;
     double* pos64B = nullptr;
-    float2* aux = nullptr;
+    float4* fin = nullptr;             // force inputs, 2 per particle (see launch_density)
     NbrList nbr;                     // neighbour list of the step (density -> force pass)
     int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
     int32_t* big_count = nullptr;     // counters[0]: big voxels, counters[1]: density tasks
@@ -106,7 +106,7 @@ struct SphgbCtx {
     // buffer capacities (elements), so reconfiguration reuses what is big enough
     struct {
         size_t scenes = 0, pbegin = 0, pipe = 0, cell = 0, slot = 0, tmp_pid = 0, vstart = 0,
-               vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, aux = 0, big_list = 0,
+               vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, fin = 0, big_list = 0,
                big_count = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
                partials = 0;
     } cap;
@@ -154,7 +154,7 @@ void free_ctx(SphgbCtx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
-                    c->pos64B, c->aux, c->owned, c->stage, c->d_chunks, c->d_partials,
+                    c->pos64B, c->fin, c->owned, c->stage, c->d_chunks, c->d_partials,
                     c->big_list, c->big_count, c->nbr.idx, c->nbr.count, c->tasks};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -458,13 +458,14 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
                               p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
     if (rc) return rc;
     if (c->density_variant == SPHGB_DENSITY_WARP)
-        SPHGB_CUDA(launch_density_wc(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr,
-                                     c->tasks, c->big_count + 1));
+        SPHGB_CUDA(launch_density_wc(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
+                                     c->nbr, c->tasks, c->big_count + 1));
     else
-        SPHGB_CUDA(launch_density(L, c->posB, c->vstart, c->vcount, c->rho, c->aux, c->nbr));
+        SPHGB_CUDA(launch_density(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
+                                  c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
     const bool sep = c->out_pos != nullptr;
-    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->aux, c->pidB, p64B, c->vstart,
+    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
                                 c->vcount, c->scene_step, c->nbr, sep ? c->out_pos : c->posA,
                                 sep ? c->out_vel : c->velA, sep ? c->out_pid : c->pidA,
                                 c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr,
@@ -537,7 +538,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     rc = rc ? rc : ensure(&c->posB, k.posB, N);
     rc = rc ? rc : ensure(&c->velB, k.velB, N);
     rc = rc ? rc : ensure(&c->pidB, k.pidB, N);
-    rc = rc ? rc : ensure(&c->aux, k.aux, N);
+    rc = rc ? rc : ensure(&c->fin, k.fin, 2 * N);
     rc = rc ? rc : ensure(&c->big_list, k.big_list, N / kMinBigVoxel + 1);
     rc = rc ? rc : ensure(&c->big_count, k.big_count, 2);
     rc = rc ? rc : ensure(&c->tasks, k.tasks, N);
@@ -940,7 +941,8 @@ int sphgb_density(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_vox
     if (ctx->n > 0 && (!d_pos_sorted || !d_rho_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
     SPHGB_CUDA(launch_density(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
-                              d_voxel_start, d_voxel_count, d_rho_out, ctx->aux, NbrList{}));
+                              nullptr, d_voxel_start, d_voxel_count, d_rho_out, nullptr,
+                              NbrList{}));
     return SPHGB_OK;
 }
 
@@ -954,9 +956,11 @@ int sphgb_forces(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_so
         return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
     const Launch L = ctx->launch(st);
-    SPHGB_CUDA(launch_aux_from_rho(L, d_rho_sorted, ctx->aux));
+    SPHGB_CUDA(launch_force_inputs(L, reinterpret_cast<const float4*>(d_pos_sorted),
+                                   reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
+                                   ctx->fin));
     SPHGB_CUDA(launch_forces(L, reinterpret_cast<const float4*>(d_pos_sorted),
-                             reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted, ctx->aux,
+                             reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted, ctx->fin,
                              d_voxel_start, d_voxel_count, reinterpret_cast<float4*>(d_pressure_out),
                              reinterpret_cast<float4*>(d_viscosity_out)));
     return SPHGB_OK;
@@ -976,10 +980,12 @@ int sphgb_integrate(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel
         return fail(SPHGB_ERR_INVALID, "pipe scenes need the FP64 position buffers");
     cudaStream_t st = as_stream(stream);
     const Launch L = ctx->launch(st);
-    SPHGB_CUDA(launch_aux_from_rho(L, d_rho_sorted, ctx->aux));
+    SPHGB_CUDA(launch_force_inputs(L, reinterpret_cast<const float4*>(d_pos_sorted),
+                                   reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
+                                   ctx->fin));
     SPHGB_CUDA(launch_integrate(L, reinterpret_cast<const float4*>(d_pos_sorted),
                                 reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
-                                ctx->aux, d_pid_sorted, d_pos64_sorted, d_voxel_start,
+                                ctx->fin, d_pid_sorted, d_pos64_sorted, d_voxel_start,
                                 d_voxel_count, d_scene_step, NbrList{},
                                 reinterpret_cast<float4*>(d_pos_out),
                                 reinterpret_cast<float4*>(d_vel_out), d_pid_out, d_pos64_out,

@@ -400,17 +400,21 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
                                const double* pos64, float4* pos_out, float4* vel_out,
                                int32_t* pid_out, double* pos64_out, int2* tasks = nullptr,
                                int32_t* task_count = nullptr);
-cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
-                           const int32_t* vcount, float* rho, float2* aux, NbrList nbr);
+// fin (optional, with vel): the force inputs of each particle, two float4
+// per particle: (x, y, z, p/rho^2) and (vx, vy, vz, 1/rho)
+cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel,
+                           const int32_t* vstart, const int32_t* vcount, float* rho,
+                           float4* fin, NbrList nbr);
 // the step's density pass: one warp per task (<= 32 particles of one voxel)
-cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
-                              const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                              const int2* tasks, const int32_t* task_count);
+cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
+                              const int32_t* vstart, const int32_t* vcount, float* rho,
+                              float4* fin, NbrList nbr, const int2* tasks,
+                              const int32_t* task_count);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
-                          const float* rho, const float2* aux, const int32_t* vstart,
+                          const float* rho, const float4* fin, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);
 cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
-                             const float* rho, const float2* aux, const int32_t* pid,
+                             const float* rho, const float4* fin, const int32_t* pid,
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
@@ -418,7 +422,9 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, int32_t* list, int stride,
                               int32_t* n_capped, int32_t* n_uncapped);
-cudaError_t launch_aux_from_rho(const Launch& L, const float* rho, float2* aux);
+// the force inputs from a given density (stage entry points)
+cudaError_t launch_force_inputs(const Launch& L, const float4* pos, const float4* vel,
+                                const float* rho, float4* fin);
 
 // generate.cu: start states and the point-field vertex stage
 cudaError_t launch_generate(const SphgbGenerator& g, const double* pipe, int pipe_rows, int64_t n,

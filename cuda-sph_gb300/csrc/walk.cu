@@ -16,20 +16,35 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // density_kernel, voxel_kernels.py:109-132: rho_i = MASS * sum_{j != i} W_ij,
 // W = W_CONST (h^2 - r^2)^3 (base_kernels.py:6-9), written here as
 // W_CONST h^6 (1 - r^2/h^2)^3 so the FP32 sum stays in range for any h.
-// Also writes aux_i = (p_i / rho_i^2, 1 / rho_i) with p = K (rho - RHO_0), the
-// per-particle factors of the force pass (voxel_kernels.py:162-164, :205-208),
+// Also writes the particle's force inputs (see write_force_inputs) with the
+// per-particle factors of the force pass, p_i / rho_i^2 and 1 / rho_i, p = K (rho
+// - RHO_0) (voxel_kernels.py:162-164, :205-208),
 // and, when nbr is given, the particle's neighbours other than itself in walk
 // order (the set every later kernel of the step uses), one row per particle,
 // nbr.idx[s * kListCap + k]; nbr.count[s] = their number, or -1 when more
 // than kListCap (the force pass then walks again).
+// Force inputs of particle s: fin[2s] = (x, y, z, p/rho^2), fin[2s + 1] =
+// (vx, vy, vz, 1/rho), one 32-byte record that the force pass reads per
+// neighbour instead of three separate arrays.
+__device__ __forceinline__ void write_force_inputs(int s, const float4& pi, const SceneDev& sc,
+                                                   const float4* __restrict__ vel, float r,
+                                                   float4* __restrict__ fin) {
+    const float p = sc.k * (r - sc.rho0);
+    const float4 v = __ldg(vel + s);
+    fin[2 * s] = make_float4(pi.x, pi.y, pi.z, p / (r * r));
+    fin[2 * s + 1] = make_float4(v.x, v.y, v.z, 1.0f / r);
+}
+
 // One particle's density by a thread-private walk: the walk records neighbour
 // slots in row[k * stride] (k < kListCap), the sum runs afterwards in walk
 // order; with more neighbours than that the walk is repeated, summing.
+// fin (with vel) is optional.
 __device__ __forceinline__ void density_one(int s, const float4& pi, const SceneDev& sc,
                                             const float4* __restrict__ pos,
+                                            const float4* __restrict__ vel,
                                             const int32_t* __restrict__ vstart,
                                             const int32_t* __restrict__ vcount, int n,
-                                            float* __restrict__ rho, float2* __restrict__ aux,
+                                            float* __restrict__ rho, float4* __restrict__ fin,
                                             const NbrList& nbr, int32_t* row, int stride) {
     const WalkGeom g = load_geom(sc);
     int others = 0;
@@ -68,10 +83,7 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
     }
     const float r = (acc.s * sc.w_const) * sc.mass;
     rho[s] = r;
-    if (aux) {
-        const float p = sc.k * (r - sc.rho0);
-        aux[s] = make_float2(p / (r * r), 1.0f / r);
-    }
+    if (fin) write_force_inputs(s, pi, sc, vel, r, fin);
     if (nbr.count) nbr.count[s] = others <= kListCap ? others : -1;
 }
 
@@ -79,14 +91,14 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
 // path of the warp-cooperative kernel below)
 __global__ void __launch_bounds__(kBlock)
 k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
-          int n, const float4* __restrict__ pos, const int32_t* __restrict__ vstart,
-          const int32_t* __restrict__ vcount, float* __restrict__ rho, float2* __restrict__ aux,
-          NbrList nbr) {
+          int n, const float4* __restrict__ pos, const float4* __restrict__ vel,
+          const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+          float* __restrict__ rho, float4* __restrict__ fin, NbrList nbr) {
     __shared__ int32_t s_list[kListCap][kBlock];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
-    density_one(s, __ldg(pos + s), sc, pos, vstart, vcount, n, rho, aux, nbr,
+    density_one(s, __ldg(pos + s), sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
                 &s_list[0][threadIdx.x], kBlock);
 }
 
@@ -144,8 +156,9 @@ struct WcShared {
 __global__ void __launch_bounds__(kWcWarps * 32)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
              int n_scenes, int n, const float4* __restrict__ pos,
-             const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
-             float* __restrict__ rho, float2* __restrict__ aux, NbrList nbr,
+             const float4* __restrict__ vel, const int32_t* __restrict__ vstart,
+             const int32_t* __restrict__ vcount, float* __restrict__ rho,
+             float4* __restrict__ fin, NbrList nbr,
              const int2* __restrict__ tasks, const int32_t* __restrict__ task_count) {
     __shared__ WcShared sh[kWcWarps];
     const unsigned full = 0xffffffffu;
@@ -168,7 +181,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home) density_one(s, pi, sc, pos, vstart, vcount, n, rho, aux, nbr, &S.list[lane][0], 1);
+            if (home) density_one(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr, &S.list[lane][0], 1);
             __syncwarp();
             continue;
         }
@@ -304,37 +317,22 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             }
             const float r = (acc.s * sc.w_const) * sc.mass;
             rho[s] = r;
-            if (aux) {
-                const float p = sc.k * (r - sc.rho0);
-                aux[s] = make_float2(p / (r * r), 1.0f / r);
-            }
+            if (fin) write_force_inputs(s, pi, sc, vel, r, fin);
             if (nbr.count) nbr.count[s] = others;
         }
         __syncwarp();
     }
 }
 
-// Row-chunk density pass.  A task is a chunk of kRowX consecutive voxels of one
-// row of the voxel table (fixed y, z; x fastest, so the chunk's particles are
-// consecutive slots).  Every walk voxel of its particles lies in one of 9 row
-// segments (y +-1, z +-1) spanning x0 - 1 .. x0 + kRowX, each again a run of
-// consecutive slots, so the block copies the whole neighbourhood into shared
-// memory with 9 coalesced copies.  Then one thread per particle walks its 27
-// voxels from shared memory exactly like walk() (same order, voxel culling,
-// FP32 test with the FP64 guard band, cap with self counted), summing its
-// density in walk order as it accepts neighbours and writing its neighbour
-// list.  Results are bit-identical to density_one.  Scenes in truncated-walk
-// mode or with a cap beyond the list, neighbourhoods beyond the shared
-// buffer and overflow buckets take density_one (global memory walk).
 __global__ void __launch_bounds__(kBlock)
-k_aux(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
-      int n, const float* __restrict__ rho, float2* __restrict__ aux) {
+k_force_inputs(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+               int n_scenes, int n, const float4* __restrict__ pos,
+               const float4* __restrict__ vel, const float* __restrict__ rho,
+               float4* __restrict__ fin) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
-    const float r = rho[s];
-    const float p = sc.k * (r - sc.rho0);
-    aux[s] = make_float2(p / (r * r), 1.0f / r);
+    write_force_inputs(s, __ldg(pos + s), sc, vel, rho[s], fin);
 }
 
 // Pressure and viscosity sums.  Compensated (Kahan) by default; kPlain sums
@@ -393,8 +391,7 @@ template <bool kPlain>
 __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4& vi,
                                            float a_i, const SceneDev& sc, const WalkGeom& geom,
                                            const float4* __restrict__ pos,
-                                           const float4* __restrict__ vel,
-                                           const float2* __restrict__ aux,
+                                           const float4* __restrict__ fin,
                                            const int32_t* __restrict__ vstart,
                                            const int32_t* __restrict__ vcount,
                                            ForceSums<kPlain>& f) {
@@ -402,7 +399,8 @@ __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
     walk(pi, geom, vstart, vcount, pos, geom.cap, [&](int j, float dx, float dy, float dz, float d2) {
         if (j == s) return;
-        add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
+        const float4 a = __ldg(fin + 2 * j), b = __ldg(fin + 2 * j + 1);
+        add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(a.w, b.w), b, dx, dy, dz, d2);
     });
 }
 
@@ -411,9 +409,7 @@ __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4
 template <bool kPlain>
 __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& vi, float a_i,
                                                 const SceneDev& sc,
-                                                const float4* __restrict__ pos,
-                                                const float4* __restrict__ vel,
-                                                const float2* __restrict__ aux,
+                                                const float4* __restrict__ fin,
                                                 const int32_t* __restrict__ list, int n, int cnt,
                                                 ForceSums<kPlain>& f) {
     const float inv_h = 1.0f / sc.h;
@@ -426,14 +422,15 @@ __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& 
         for (int u = 0; u < 4; ++u) {
             if (k0 + u >= cnt) break;
             const int j = js[u];
-            const float4 pj = __ldg(pos + j);
+            const float4 pj = __ldg(fin + 2 * j);       // position, p/rho^2
+            const float4 vj = __ldg(fin + 2 * j + 1);   // velocity, 1/rho
             const float dx = __fsub_rn(pi.x, pj.x);
             const float dy = __fsub_rn(pi.y, pj.y);
             const float dz = __fsub_rn(pi.z, pj.z);
             float d2 = __fmul_rn(dx, dx);
             d2 = __fmaf_rn(dy, dy, d2);
             d2 = __fmaf_rn(dz, dz, d2);
-            add_pair(f, vi, a_i, inv_h, gw, lw, __ldg(aux + j), __ldg(vel + j), dx, dy, dz, d2);
+            add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(pj.w, vj.w), vj, dx, dy, dz, d2);
         }
     }
 }
@@ -449,8 +446,7 @@ struct Forces {
 __device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float4& vi,
                                             const float2& ai, const SceneDev& sc,
                                             const float4* __restrict__ pos,
-                                            const float4* __restrict__ vel,
-                                            const float2* __restrict__ aux,
+                                            const float4* __restrict__ fin,
                                             const int32_t* __restrict__ vstart,
                                             const int32_t* __restrict__ vcount,
                                             const int32_t* __restrict__ list, int n, int cnt) {
@@ -458,15 +454,15 @@ __device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float
     bool plain = !(fabsf(ai.x * ai.y) < INFINITY);
     if (!plain) {
         ForceSums<false> f;
-        if (cnt >= 0) force_sums_list<false>(pi, vi, ai.x, sc, pos, vel, aux, list, n, cnt, f);
-        else force_sums<false>(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+        if (cnt >= 0) force_sums_list<false>(pi, vi, ai.x, sc, fin, list, n, cnt, f);
+        else force_sums<false>(s, pi, vi, ai.x, sc, load_geom(sc), pos, fin, vstart, vcount, f);
         out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
         plain = f.bad;
     }
     if (plain) {
         ForceSums<true> f;
-        if (cnt >= 0) force_sums_list<true>(pi, vi, ai.x, sc, pos, vel, aux, list, n, cnt, f);
-        else force_sums<true>(s, pi, vi, ai.x, sc, load_geom(sc), pos, vel, aux, vstart, vcount, f);
+        if (cnt >= 0) force_sums_list<true>(pi, vi, ai.x, sc, fin, list, n, cnt, f);
+        else force_sums<true>(s, pi, vi, ai.x, sc, load_geom(sc), pos, fin, vstart, vcount, f);
         out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
     }
     return out;
@@ -484,7 +480,7 @@ __device__ __forceinline__ float visc_term(const Forces& f, int a, float vscale)
 __global__ void __launch_bounds__(kBlock)
 k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
          int n, const float4* __restrict__ pos, const float4* __restrict__ vel,
-         const float2* __restrict__ aux, const int32_t* __restrict__ vstart,
+         const float4* __restrict__ fin, const int32_t* __restrict__ vstart,
          const int32_t* __restrict__ vcount, float4* __restrict__ pressure,
          float4* __restrict__ viscosity) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -492,8 +488,8 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
     const float4 pi = __ldg(pos + s);
     const float4 vi = __ldg(vel + s);
-    const float2 ai = __ldg(aux + s);
-    const Forces f = forces_of(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount, nullptr, n, -1);
+    const float2 ai = make_float2(__ldg(fin + 2 * s).w, __ldg(fin + 2 * s + 1).w);
+    const Forces f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, nullptr, n, -1);
     const float vscale = sc.mass * sc.visc * ai.y;
     pressure[s] = make_float4(f.p[0], f.p[1], f.p[2], 0.0f);
     viscosity[s] = make_float4(visc_term(f, 0, vscale), visc_term(f, 1, vscale),
@@ -509,7 +505,7 @@ __global__ void __launch_bounds__(kBlock, kPipe ? 1 : 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
             const float4* __restrict__ vel, const float* __restrict__ rho,
-            const float2* __restrict__ aux, const int32_t* __restrict__ pid,
+            const float4* __restrict__ fin, const int32_t* __restrict__ pid,
             const double* __restrict__ pos64, const int32_t* __restrict__ vstart,
             const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
             NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
@@ -521,10 +517,10 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const SceneDev& sc = scenes[si];
     const float4 pi = __ldg(pos + s);
     const float4 vi = __ldg(vel + s);
-    const float2 ai = __ldg(aux + s);
+    const float2 ai = make_float2(__ldg(fin + 2 * s).w, __ldg(fin + 2 * s + 1).w);
     const float rho_i = __ldg(rho + s);
     const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
-    const Forces f = forces_of(s, pi, vi, ai, sc, pos, vel, aux, vstart, vcount,
+    const Forces f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount,
                                nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr, n, cnt);
     const float vscale = sc.mass * sc.visc * ai.y;
     // result_force = ext + -P + V (base_kernels.py:46-52)
@@ -598,46 +594,50 @@ k_neighbours(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
 
 }  // namespace
 
-cudaError_t launch_density(const Launch& L, const float4* pos, const int32_t* vstart,
-                           const int32_t* vcount, float* rho, float2* aux, NbrList nbr) {
+cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel,
+                           const int32_t* vstart, const int32_t* vcount, float* rho,
+                           float4* fin, NbrList nbr) {
     if (L.n == 0) return cudaSuccess;
     k_density<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                         vstart, vcount, rho, aux, nbr);
+                                                         vel, vstart, vcount, rho, fin, nbr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_density_wc(const Launch& L, const float4* pos, const int32_t* vstart,
-                              const int32_t* vcount, float* rho, float2* aux, NbrList nbr,
-                              const int2* tasks, const int32_t* task_count) {
+cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
+                              const int32_t* vstart, const int32_t* vcount, float* rho,
+                              float4* fin, NbrList nbr, const int2* tasks,
+                              const int32_t* task_count) {
     if (L.n == 0) return cudaSuccess;
     // persistent grid: up to 4 blocks of 8 warps per SM, warps stride over the tasks
     int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
     if (blocks > 152 * 4) blocks = 152 * 4;
     k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                         vstart, vcount, rho, aux, nbr, tasks,
+                                                         vel, vstart, vcount, rho, fin, nbr, tasks,
                                                          task_count);
     return cudaGetLastError();
 }
 
-cudaError_t launch_aux_from_rho(const Launch& L, const float* rho, float2* aux) {
+cudaError_t launch_force_inputs(const Launch& L, const float4* pos, const float4* vel,
+                                const float* rho, float4* fin) {
     if (L.n == 0) return cudaSuccess;
-    k_aux<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, rho, aux);
+    k_force_inputs<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n,
+                                                              pos, vel, rho, fin);
     return cudaGetLastError();
 }
 
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
-                          const float* rho, const float2* aux, const int32_t* vstart,
+                          const float* rho, const float4* fin, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity) {
     (void)rho;
     if (L.n == 0) return cudaSuccess;
     k_forces<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                        vel, aux, vstart, vcount, pressure,
+                                                        vel, fin, vstart, vcount, pressure,
                                                         viscosity);
     return cudaGetLastError();
 }
 
 cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
-                             const float* rho, const float2* aux, const int32_t* pid,
+                             const float* rho, const float4* fin, const int32_t* pid,
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
@@ -645,11 +645,11 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
     if (L.n == 0) return cudaSuccess;
     if (L.pipe_scenes)
         k_integrate<true><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
     else
         k_integrate<false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, aux, pid, pos64, vstart,
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
     return cudaGetLastError();
 }

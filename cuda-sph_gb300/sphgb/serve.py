@@ -38,9 +38,9 @@ from .device import SceneBatch, SceneSpec
 
 # HBM bytes per particle for a scene resident in the batch: bound state
 # (pos, vel 16 B each, rho, pid 4 B), the step's sorted copies (36 B), ids and
-# ranks (12 B), aux (8 B), neighbour list (132 B), density tasks (8 B), export
-# staging (56 B) and the FP64 accumulator (48 B both buffers, pipe scenes)
-BYTES_PER_PARTICLE = 40 + 36 + 12 + 8 + 132 + 8 + 56
+# ranks (12 B), force inputs (32 B), neighbour list (132 B), density tasks (8 B),
+# export staging (56 B) and the FP64 accumulator (48 B both buffers, pipe scenes)
+BYTES_PER_PARTICLE = 40 + 36 + 12 + 32 + 132 + 8 + 56
 BYTES_PER_PIPE_PARTICLE = 48
 BYTES_PER_VOXEL = 8
 
