@@ -145,22 +145,13 @@ constexpr int kSelfTerm = 0x7fc0dead;
 constexpr int kWcList = kListCap;       // accepted neighbours per particle, self included
 
 struct WcShared {
+    float4 home[32];
     ulonglong2 home_xy[32];   // (x, x), (y, y) of each home particle, packed
     f32x2 home_z[32];         // (z, z)
     int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
     int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
     int32_t st[27];     // first slot of each walk voxel
 };
-
-// home particle i's position from its packed copies
-__device__ __forceinline__ float4 home_of(const WcShared& S, int i) {
-    const ulonglong2 xy = S.home_xy[i];
-    float x, y, z, unused;
-    f2unpack(xy.x, x, unused);
-    f2unpack(xy.y, y, unused);
-    f2unpack(S.home_z[i], z, unused);
-    return make_float4(x, y, z, 0.0f);
-}
 
 __global__ void __launch_bounds__(kWcWarps * 32)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
@@ -195,6 +186,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             continue;
         }
         if (home) {
+            S.home[lane] = pi;
             S.home_xy[lane] = make_ulonglong2(f2pack(pi.x, pi.x), f2pack(pi.y, pi.y));
             S.home_z[lane] = f2pack(pi.z, pi.z);
         }
@@ -269,7 +261,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                 bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
                 const bool band0 = !acc0 && d20 <= h2_hi, band1 = !acc1 && d21 <= h2_hi;
                 if (__any_sync(full, band0 || band1)) {
-                    const float4 ph = home_of(S, i);
+                    const float4 ph = S.home[i];
                     if (band0) acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
                     if (band1) acc1 = within_exact(ph.x, ph.y, ph.z, pj1.x, pj1.y, pj1.z, h_d);
                 }
@@ -295,7 +287,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             if (in) {
                 int term = kSelfTerm;
                 if (j != si) {
-                    const float4 ph = home_of(S, i);
+                    const float4 ph = S.home[i];
                     const float4 pj = __ldg(pos + j);
                     const float dx = __fsub_rn(ph.x, pj.x);
                     const float dy = __fsub_rn(ph.y, pj.y);
