@@ -68,6 +68,7 @@ struct SphgbCtx {
     int n_pipe_rows = 0;
     // scratch
     int32_t* cell = nullptr;
+    int32_t* slot_of = nullptr;        // original index -> sorted slot (AoS export)
     int32_t* slot = nullptr;
     int32_t* tmp_pid = nullptr;
     int32_t* vstart = nullptr;
@@ -105,7 +106,8 @@ struct SphgbCtx {
     double* d_partials = nullptr;
     // buffer capacities (elements), so reconfiguration reuses what is big enough
     struct {
-        size_t scenes = 0, pbegin = 0, pipe = 0, cell = 0, slot = 0, tmp_pid = 0, vstart = 0,
+        size_t scenes = 0, pbegin = 0, pipe = 0, cell = 0, slot_of = 0, slot = 0, tmp_pid = 0,
+               vstart = 0,
                vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, fin = 0, big_list = 0,
                big_count = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
                partials = 0;
@@ -152,7 +154,7 @@ int dalloc(T** p, size_t count) {
 void free_ctx(SphgbCtx* c) {
     if (!c) return;
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-    void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot, c->tmp_pid,
+    void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot_of, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->fin, c->owned, c->stage, c->d_chunks, c->d_partials,
                     c->big_list, c->big_count, c->nbr.idx, c->nbr.count, c->tasks};
@@ -262,16 +264,26 @@ __global__ void k_load_aos(const SceneDev* __restrict__ scenes, const int32_t* _
     (void)scenes;
 }
 
+// slot_of[original index] = sorted slot (the inverse of the particle ids)
+__global__ void k_slot_of(const int32_t* __restrict__ pbegin, int n_scenes, int n,
+                          const int32_t* __restrict__ pid, int32_t* __restrict__ slot_of) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    slot_of[__ldg(pbegin + scene_of(s, pbegin, n_scenes)) + pid[s]] = s;
+}
+
+// state in original particle order as FP64 AoS: one thread per output row,
+// so the writes are coalesced (they may go to mapped host memory)
 __global__ void k_store_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
                             int n_scenes, int n, const float4* __restrict__ pos,
                             const float4* __restrict__ vel, const float* __restrict__ rho,
-                            const int32_t* __restrict__ pid, const double* __restrict__ pos64,
+                            const int32_t* __restrict__ slot_of, const double* __restrict__ pos64,
                             double* __restrict__ pos_out, double* __restrict__ vel_out,
                             double* __restrict__ rho_out) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const int si = scene_of(s, pbegin, n_scenes);
-    const int i = __ldg(pbegin + si) + pid[s];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int si = scene_of(i, pbegin, n_scenes);
+    const int s = __ldg(slot_of + i);
     if (pos_out) {
         if (pos64 && scenes[si].mode == 1) {
             pos_out[3 * i] = pos64[3 * s];
@@ -421,6 +433,17 @@ __global__ void k_philox(uint64_t seed, const int32_t* pid, int n, int step, int
 
 inline int blocks(int n, int b = kBlock) { return (n + b - 1) / b; }
 
+// device address of page-locked, device-mapped host memory; nullptr for any
+// other pointer (pageable host memory, device memory)
+const void* device_view(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();   // clear the error of an unknown pointer
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // hash + scan + scatter + big-voxel sort + rank-gather: state (any order) ->
@@ -530,6 +553,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     rc = rc ? rc : ensure(&c->d_pbegin, k.pbegin, (size_t)n_scenes + 1);
     rc = rc ? rc : ensure(&c->d_pipe, k.pipe, (size_t)n_pipe_rows_total * 5);
     rc = rc ? rc : ensure(&c->cell, k.cell, N);
+    rc = rc ? rc : ensure(&c->slot_of, k.slot_of, N);
     rc = rc ? rc : ensure(&c->slot, k.slot, N);
     rc = rc ? rc : ensure(&c->tmp_pid, k.tmp_pid, N);
     rc = rc ? rc : ensure(&c->vstart, k.vstart, V);
@@ -731,9 +755,11 @@ int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
     cudaStream_t st = as_stream(stream);
     // the latest step's result: the output buffers when bound, else the state
     const bool sep = ctx->out_pos != nullptr;
+    k_slot_of<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                                 sep ? ctx->out_pid : ctx->pidA, ctx->slot_of);
     k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(
         ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sep ? ctx->out_pos : ctx->posA,
-        sep ? ctx->out_vel : ctx->velA, ctx->rho, sep ? ctx->out_pid : ctx->pidA,
+        sep ? ctx->out_vel : ctx->velA, ctx->rho, ctx->slot_of,
         sep ? ctx->out_pos64 : ctx->pos64A, d_pos_aos, d_vel_aos, d_rho);
     SPHGB_CUDA(cudaGetLastError());
     return SPHGB_OK;
@@ -843,17 +869,32 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     double* sp = ctx->stage;
     double* sv = ctx->stage + 3 * N;
     double* sr = ctx->stage + 6 * N;
-    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-    int rc = sphgb_ctx_load_aos_f64(ctx, sp, sv, st);
+    // Page-locked host arrays that the device can address are read and written
+    // by the load and store kernels directly (over the host link); any other
+    // host memory goes through the device staging buffers with copies.
+    const double* in_p = static_cast<const double*>(device_view(h_pos));
+    const double* in_v = static_cast<const double*>(device_view(h_vel));
+    if (!in_p || !in_v) {
+        SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+        SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+        in_p = sp;
+        in_v = sv;
+    }
+    int rc = sphgb_ctx_load_aos_f64(ctx, in_p, in_v, st);
     if (rc) return rc;
     rc = enqueue_step(ctx, st);
     if (rc) return rc;
-    rc = sphgb_ctx_store_aos_f64(ctx, sp, sv, sr, st);
+    double* out_p = static_cast<double*>(device_view(h_pos_out));
+    double* out_v = static_cast<double*>(device_view(h_vel_out));
+    double* out_r = static_cast<double*>(device_view(h_rho_out));
+    const bool direct = out_p && out_v && out_r;
+    rc = sphgb_ctx_store_aos_f64(ctx, direct ? out_p : sp, direct ? out_v : sv, direct ? out_r : sr, st);
     if (rc) return rc;
-    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    if (!direct) {
+        SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+        SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+        SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    }
     SPHGB_CUDA(cudaStreamSynchronize(st));
     return SPHGB_OK;
 }

@@ -153,7 +153,7 @@ struct WcShared {
     int32_t st[27];     // first slot of each walk voxel
 };
 
-__global__ void __launch_bounds__(kWcWarps * 32)
+__global__ void __launch_bounds__(kWcWarps * 32, 4)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
              int n_scenes, int n, const float4* __restrict__ pos,
              const float4* __restrict__ vel, const int32_t* __restrict__ vstart,

@@ -107,12 +107,17 @@ class AsyncFrameSaver:
         self._stream.wait_stream(producer)
         with torch.cuda.stream(self._stream):
             dp, dv, dr = scenes.export_aos_f64(stream=self._stream)
+            # the next steps rewrite the state in place: they wait for the
+            # export (a short kernel), not for the copies to the host
+            exported = torch.cuda.Event()
+            exported.record(self._stream)
             lo = scenes.scene_offsets[index]
             hp.copy_(dp[lo:lo + n], non_blocking=True)
             hv.copy_(dv[lo:lo + n], non_blocking=True)
             hr.copy_(dr[lo:lo + n], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(self._stream)
+        producer.wait_event(exported)
         self._todo.put((self._epoch, ev, (hp, hv, hr)))
         self._epoch += 1
 

@@ -222,3 +222,28 @@ def test_density_variants_identical_on_dense_voxels():
         for o in outs[1:]:
             np.testing.assert_array_equal(o.density, outs[0].density)
             np.testing.assert_array_equal(o.velocity, outs[0].velocity)
+
+
+def test_host_entry_page_locked_buffers_match_pageable():
+    """sphgb_compute_next_state_host reads and writes page-locked host arrays
+    directly from the kernels; the result is the same bits as through the
+    staging copies used for pageable arrays."""
+    torch = torch_cuda()
+    from sphgb import scenes
+    from sphgb.device import SceneBatch
+    for spec, st in (scenes.config0(), scenes.pipe_flow(n=20_000, seed=11,
+                                                         h=0.02 * (262_144 / 20_000) ** (1 / 3))):
+        n = spec.n
+        b = SceneBatch([spec])
+        pageable = b.compute_next_state_host(np.array(st.position), np.array(st.velocity))
+        pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa
+        hp, hv = pin((n, 3)), pin((n, 3))
+        hp[:] = st.position
+        hv[:] = st.velocity
+        op, ov, orho = pin((n, 3)), pin((n, 3)), pin((n,))
+        locked = b.compute_next_state_host(hp, hv, op, ov, orho)
+        for a, c in zip(pageable, locked):
+            np.testing.assert_array_equal(a, c)
+        np.testing.assert_array_equal(op, pageable[0])
+        np.testing.assert_array_equal(orho, pageable[2])
+        b.close()
