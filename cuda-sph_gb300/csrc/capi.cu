@@ -435,7 +435,7 @@ inline int blocks(int n, int b = kBlock) { return (n + b - 1) / b; }
 
 // device address of page-locked, device-mapped host memory; nullptr for any
 // other pointer (pageable host memory, device memory)
-const void* device_view(const void* p) {
+void* device_view(const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();   // clear the error of an unknown pointer
