@@ -234,8 +234,11 @@ def test_host_entry_page_locked_buffers_match_pageable():
     for spec, st in (scenes.config0(), scenes.pipe_flow(n=20_000, seed=11,
                                                          h=0.02 * (262_144 / 20_000) ** (1 / 3))):
         n = spec.n
+        # a fresh context for each call: the step index keys the pipe's respawn draws
+        a = SceneBatch([spec])
+        pageable = a.compute_next_state_host(np.array(st.position), np.array(st.velocity))
+        a.close()
         b = SceneBatch([spec])
-        pageable = b.compute_next_state_host(np.array(st.position), np.array(st.velocity))
         pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()  # noqa
         hp, hv = pin((n, 3)), pin((n, 3))
         hp[:] = st.position
