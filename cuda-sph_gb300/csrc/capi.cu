@@ -433,16 +433,6 @@ __global__ void k_philox(uint64_t seed, const int32_t* pid, int n, int step, int
 
 inline int blocks(int n, int b = kBlock) { return (n + b - 1) / b; }
 
-// device address of page-locked, device-mapped host memory; nullptr for any
-// other pointer (pageable host memory, device memory)
-void* device_view(const void* p) {
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();   // clear the error of an unknown pointer
-        return nullptr;
-    }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
 
 cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
@@ -869,32 +859,17 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     double* sp = ctx->stage;
     double* sv = ctx->stage + 3 * N;
     double* sr = ctx->stage + 6 * N;
-    // Page-locked host arrays that the device can address are read and written
-    // by the load and store kernels directly (over the host link); any other
-    // host memory goes through the device staging buffers with copies.
-    const double* in_p = static_cast<const double*>(device_view(h_pos));
-    const double* in_v = static_cast<const double*>(device_view(h_vel));
-    if (!in_p || !in_v) {
-        SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-        SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-        in_p = sp;
-        in_v = sv;
-    }
-    int rc = sphgb_ctx_load_aos_f64(ctx, in_p, in_v, st);
+    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    int rc = sphgb_ctx_load_aos_f64(ctx, sp, sv, st);
     if (rc) return rc;
     rc = enqueue_step(ctx, st);
     if (rc) return rc;
-    double* out_p = static_cast<double*>(device_view(h_pos_out));
-    double* out_v = static_cast<double*>(device_view(h_vel_out));
-    double* out_r = static_cast<double*>(device_view(h_rho_out));
-    const bool direct = out_p && out_v && out_r;
-    rc = sphgb_ctx_store_aos_f64(ctx, direct ? out_p : sp, direct ? out_v : sv, direct ? out_r : sr, st);
+    rc = sphgb_ctx_store_aos_f64(ctx, sp, sv, sr, st);
     if (rc) return rc;
-    if (!direct) {
-        SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-        SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-        SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
-    }
+    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
     SPHGB_CUDA(cudaStreamSynchronize(st));
     return SPHGB_OK;
 }

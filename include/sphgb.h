@@ -162,10 +162,8 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
  * AoS state out, synchronous (AbstractSPHStrategy.compute_next_state,
  * abstract_sph_strategy.py:31-46, including its host<->device copies at
  * :65-74 and :77-84).  Context must hold exactly one scene.  Host buffers may
- * be pageable or page-locked.  Page-locked buffers that the device can address
- * (cudaHostAlloc, or cudaHostRegister with cudaHostRegisterMapped) are read
- * and written by the kernels directly over the host link, with no staging
- * copy; others go through device staging buffers. */
+ * be pageable or page-locked (page-locked copies faster); they are copied
+ * through device staging buffers. */
 int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
                                   double* h_pos_out, double* h_vel_out, double* h_rho_out);
 

@@ -225,9 +225,8 @@ def test_density_variants_identical_on_dense_voxels():
 
 
 def test_host_entry_page_locked_buffers_match_pageable():
-    """sphgb_compute_next_state_host reads and writes page-locked host arrays
-    directly from the kernels; the result is the same bits as through the
-    staging copies used for pageable arrays."""
+    """sphgb_compute_next_state_host gives the same bits from page-locked
+    host arrays as from pageable ones."""
     torch = torch_cuda()
     from sphgb import scenes
     from sphgb.device import SceneBatch
