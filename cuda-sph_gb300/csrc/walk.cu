@@ -1,9 +1,11 @@
-// walk.cu -- neighbour walk kernels: density, forces, fused force + integrate +
-// wall response, and the neighbour list/count kernel used for parity.
+// walk.cu -- neighbour walk kernels: density (warp-cooperative for the step,
+// thread per particle for the stage entry points), forces, fused force +
+// integrate + wall response, and the neighbour list/count kernel used for
+// parity.
 //
-// One thread per particle in voxel-sorted order, so that the threads of a
-// block walk overlapping voxel neighbourhoods and their candidate loads are
-// served from L1.  The walk order and the 32-neighbour cap are the reference's
+// Particles are in voxel-sorted order, so the threads or warps of a block walk
+// overlapping voxel neighbourhoods and their candidate loads are served from
+// L1.  The walk order and the 32-neighbour cap are the reference's
 // (get_neighbours, sim/src/sph/kernels/voxel_kernels.py:30-85).
 #include "sphgb_internal.cuh"
 
@@ -130,14 +132,15 @@ __device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
 
 // Warp-cooperative density pass of the step.  One warp per task: up to 32
 // particles of one voxel (tasks listed by the rank-gather).  The 27 walk
-// voxels of that voxel are laid end to end in walk order; each batch of 32
-// candidates is loaded coalesced, one per lane, and every home particle is
-// tested against the whole batch at once: a ballot gives its accepted
-// candidates in walk order and popc ranks them against the cap, so the
-// accepted set is exactly the reference's first MAX_NEIGHBOURS (self
-// included).  Then each home particle sums its density over that list in
-// walk order with the same arithmetic as density_one: the results are
-// bit-identical to the thread-per-particle kernel.
+// voxels of that voxel are laid end to end in walk order; each batch of 64
+// candidates is loaded coalesced, two per lane, and every home particle is
+// tested against the whole batch at once (distances as packed FP32 pairs): a
+// ballot gives its accepted candidates in walk order and popc ranks them
+// against the cap, so the accepted set is exactly the reference's first
+// MAX_NEIGHBOURS (self included).  Then the density terms are computed with
+// one lane per list entry and summed in walk order with one lane per home
+// particle, the arithmetic of density_one: the results are bit-identical to
+// the thread-per-particle kernel.
 constexpr int kWcWarps = 8;
 // list entry of the particle itself once entries hold density terms: a NaN
 // bit pattern, which no term (a cube of a finite number) takes
