@@ -104,40 +104,24 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
                 &s_list[0][threadIdx.x], kBlock);
 }
 
-// ---- packed FP32 pairs (PTX .f32x2; each half rounds like the scalar op) ----
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 f2pack(float lo, float hi) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2unpack(f32x2 v, float& lo, float& hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2 f2sub(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2mul(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2fma(f32x2 a, f32x2 b, f32x2 c) {
-    f32x2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
+// squared distance with the walk's arithmetic (within() in sphgb_internal.cuh)
+__device__ __forceinline__ float dist2(const float4& a, const float4& b) {
+    const float dx = __fsub_rn(a.x, b.x);
+    const float dy = __fsub_rn(a.y, b.y);
+    const float dz = __fsub_rn(a.z, b.z);
+    float d2 = __fmul_rn(dx, dx);
+    d2 = __fmaf_rn(dy, dy, d2);
+    return __fmaf_rn(dz, dz, d2);
 }
 
 // Warp-cooperative density pass of the step.  One warp per task: up to 32
 // particles of one voxel (tasks listed by the rank-gather).  The 27 walk
 // voxels of that voxel are laid end to end in walk order; each batch of 64
 // candidates is loaded coalesced, two per lane, and every home particle is
-// tested against the whole batch at once (distances as packed FP32 pairs): a
-// ballot gives its accepted candidates in walk order and popc ranks them
-// against the cap, so the accepted set is exactly the reference's first
-// MAX_NEIGHBOURS (self included).  Then the density terms are computed with
+// tested against the whole batch at once: a ballot gives its accepted
+// candidates in walk order and popc ranks them against the cap, so the
+// accepted set is exactly the reference's first MAX_NEIGHBOURS (self
+// included).  Then the density terms are computed with
 // one lane per list entry and summed in walk order with one lane per home
 // particle, the arithmetic of density_one: the results are bit-identical to
 // the thread-per-particle kernel.
@@ -149,8 +133,6 @@ constexpr int kWcList = kListCap;       // accepted neighbours per particle, sel
 
 struct WcShared {
     float4 home[32];
-    ulonglong2 home_xy[32];   // (x, x), (y, y) of each home particle, packed
-    f32x2 home_z[32];         // (z, z)
     int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
     int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
     int32_t st[27];     // first slot of each walk voxel
@@ -188,11 +170,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             __syncwarp();
             continue;
         }
-        if (home) {
-            S.home[lane] = pi;
-            S.home_xy[lane] = make_ulonglong2(f2pack(pi.x, pi.x), f2pack(pi.y, pi.y));
-            S.home_z[lane] = f2pack(pi.z, pi.z);
-        }
+        if (home) S.home[lane] = pi;
         // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
         int ck = 0, stk = 0;
         if (lane < 27) {
@@ -218,8 +196,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
         const double h_d = sc.h_d;
         int cnt = 0;    // lane i: accepted candidates of home particle i so far
-        // 64 candidates per batch, two per lane (q0 = b0 + lane, q1 = q0 + 32),
-        // their distances computed as packed FP32 pairs
+        // 64 candidates per batch, two per lane (q0 = b0 + lane, q1 = q0 + 32)
         for (int b0 = 0; b0 < M; b0 += 64) {
             const int q0 = b0 + lane, q1 = q0 + 32;
             const bool v0 = q0 < M, v1 = q1 < M;
@@ -245,35 +222,48 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                 sj1 = S.st[lo] + (q1 - S.P[lo]);
                 pj1 = __ldg(pos + sj1);
             }
-            const f32x2 cx = f2pack(pj0.x, pj1.x), cy = f2pack(pj0.y, pj1.y),
-                        cz = f2pack(pj0.z, pj1.z);
             // home particles still below the cap
-            unsigned todo = __ballot_sync(full, home && cnt < cap);
+            const unsigned todo = __ballot_sync(full, home && cnt < cap);
             if (!todo) break;
-            while (todo) {
-                const int i = __ffs(todo) - 1;
-                todo &= todo - 1;
+            // Fast pass: FP32 decisions only.  A pair in the FP32 guard band
+            // around h^2 is rare; if any occurs, the whole batch is redone from
+            // the counts it started with, deciding those pairs in FP64.  Every
+            // list entry below the final counts is rewritten by the redo.
+            const int cnt0 = cnt;
+            bool band_seen = false;
+            for (unsigned t = todo; t; t &= t - 1) {
+                const int i = __ffs(t) - 1;
                 const int ci = __shfl_sync(full, cnt, i);
-                const ulonglong2 hxy = S.home_xy[i];
-                const f32x2 dx = f2sub(hxy.x, cx), dy = f2sub(hxy.y, cy), dz = f2sub(S.home_z[i], cz);
-                f32x2 d2p = f2mul(dx, dx);
-                d2p = f2fma(dy, dy, d2p);
-                d2p = f2fma(dz, dz, d2p);
-                float d20, d21;
-                f2unpack(d2p, d20, d21);
-                bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
-                const bool band0 = !acc0 && d20 <= h2_hi, band1 = !acc1 && d21 <= h2_hi;
-                if (__any_sync(full, band0 || band1)) {
-                    const float4 ph = S.home[i];
-                    if (band0) acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
-                    if (band1) acc1 = within_exact(ph.x, ph.y, ph.z, pj1.x, pj1.y, pj1.z, h_d);
-                }
+                const float4 ph = S.home[i];
+                const float d20 = dist2(ph, pj0), d21 = dist2(ph, pj1);
+                const bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
+                band_seen |= (!acc0 && d20 <= h2_hi) || (!acc1 && d21 <= h2_hi);
                 const unsigned m0 = __ballot_sync(full, acc0), m1 = __ballot_sync(full, acc1);
                 const int n0 = __popc(m0);
                 const int r0 = ci + __popc(m0 & lt), r1 = ci + n0 + __popc(m1 & lt);
                 if (acc0 && r0 < cap) S.list[i][r0] = sj0;
                 if (acc1 && r1 < cap) S.list[i][r1] = sj1;
                 if (lane == i) cnt = ci + n0 + __popc(m1);
+            }
+            if (__any_sync(full, band_seen)) {
+                cnt = cnt0;
+                for (unsigned t = todo; t; t &= t - 1) {
+                    const int i = __ffs(t) - 1;
+                    const int ci = __shfl_sync(full, cnt, i);
+                    const float4 ph = S.home[i];
+                    const float d20 = dist2(ph, pj0), d21 = dist2(ph, pj1);
+                    bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
+                    if (!acc0 && d20 <= h2_hi)
+                        acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
+                    if (!acc1 && d21 <= h2_hi)
+                        acc1 = within_exact(ph.x, ph.y, ph.z, pj1.x, pj1.y, pj1.z, h_d);
+                    const unsigned m0 = __ballot_sync(full, acc0), m1 = __ballot_sync(full, acc1);
+                    const int n0 = __popc(m0);
+                    const int r0 = ci + __popc(m0 & lt), r1 = ci + n0 + __popc(m1 & lt);
+                    if (acc0 && r0 < cap) S.list[i][r0] = sj0;
+                    if (acc1 && r1 < cap) S.list[i][r1] = sj1;
+                    if (lane == i) cnt = ci + n0 + __popc(m1);
+                }
             }
         }
         __syncwarp();
@@ -290,14 +280,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             if (in) {
                 int term = kSelfTerm;
                 if (j != si) {
-                    const float4 ph = S.home[i];
-                    const float4 pj = __ldg(pos + j);
-                    const float dx = __fsub_rn(ph.x, pj.x);
-                    const float dy = __fsub_rn(ph.y, pj.y);
-                    const float dz = __fsub_rn(ph.z, pj.z);
-                    float d2 = __fmul_rn(dx, dx);
-                    d2 = __fmaf_rn(dy, dy, d2);
-                    d2 = __fmaf_rn(dz, dz, d2);
+                    const float d2 = dist2(S.home[i], __ldg(pos + j));
                     const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
                     term = __float_as_int(u * u * u);
                     if (nbr.idx) nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
