@@ -116,8 +116,10 @@ __device__ __forceinline__ float dist2(const float4& a, const float4& b) {
 
 // Warp-cooperative density pass of the step.  One warp per task: up to 32
 // particles of one voxel (tasks listed by the rank-gather).  The 27 walk
-// voxels of that voxel are laid end to end in walk order; each batch of 64
-// candidates is loaded coalesced, two per lane, and every home particle is
+// voxels of that voxel are laid end to end in walk order; each batch of 96
+// candidates is loaded coalesced, three per lane (a candidate's slot found
+// from voxel-boundary bit masks built with one warp OR-reduction per 32
+// candidates), and every home particle is
 // tested against the whole batch at once: a ballot gives its accepted
 // candidates in walk order and popc ranks them against the cap, so the
 // accepted set is exactly the reference's first MAX_NEIGHBOURS (self
@@ -130,12 +132,13 @@ constexpr int kWcWarps = 8;
 // bit pattern, which no term (a cube of a finite number) takes
 constexpr int kSelfTerm = 0x7fc0dead;
 constexpr int kWcList = kListCap;       // accepted neighbours per particle, self included
+constexpr int kWcPerLane = 3;           // candidates per lane in one batch
+constexpr int kWcBatch = 32 * kWcPerLane;
 
 struct WcShared {
     float4 home[32];
     int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
-    int32_t P[28];      // exclusive prefix of the walk voxels' counts (P[27] = total)
-    int32_t st[27];     // first slot of each walk voxel
+    int32_t off[27];    // first slot - first walk index of each non-empty walk voxel, by rank
 };
 
 __global__ void __launch_bounds__(kWcWarps * 32, 4)
@@ -190,41 +193,50 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             const int v = __shfl_up_sync(full, incl, o);
             if (lane >= o) incl += v;
         }
-        if (lane < 27) { S.P[lane] = incl - ck; S.st[lane] = stk; }
-        const int M = __shfl_sync(full, incl, 26);
+        const int M = __shfl_sync(full, incl, 26);   // candidates in the whole walk
+        // Candidate q (walk order) lies in the non-empty walk voxel with the
+        // largest first index P_k <= q; its slot is q + (start_k - P_k).  Lane
+        // k keeps P_k; S.off holds start_k - P_k by rank among the non-empty
+        // walk voxels.
+        const int Pk = incl - ck;
+        const bool nzk = lane < 27 && ck > 0;
+        const unsigned NZ = __ballot_sync(full, nzk);
+        if (nzk) S.off[__popc(NZ & lt)] = stk - Pk;
         __syncwarp();
         const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
         const double h_d = sc.h_d;
+        const float inf = __int_as_float(0x7f800000);
+        const unsigned le = (2u << lane) - 1u;      // bits 0..lane
         int cnt = 0;    // lane i: accepted candidates of home particle i so far
-        // 64 candidates per batch, two per lane (q0 = b0 + lane, q1 = q0 + 32)
-        for (int b0 = 0; b0 < M; b0 += 64) {
-            const int q0 = b0 + lane, q1 = q0 + 32;
-            const bool v0 = q0 < M, v1 = q1 < M;
-            // past the end of the walk: +inf coordinates, never within h
-            const float inf = __int_as_float(0x7f800000);
-            float4 pj0 = make_float4(inf, inf, inf, 0.f), pj1 = pj0;
-            int sj0 = -1, sj1 = -1;
-            if (v0) {
-                int lo = 0, hi = 26;            // last walk voxel with P <= q
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.P[mid] <= q0) lo = mid; else hi = mid - 1;
-                }
-                sj0 = S.st[lo] + (q0 - S.P[lo]);
-                pj0 = __ldg(pos + sj0);
-            }
-            if (v1) {
-                int lo = 0, hi = 26;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.P[mid] <= q1) lo = mid; else hi = mid - 1;
-                }
-                sj1 = S.st[lo] + (q1 - S.P[lo]);
-                pj1 = __ldg(pos + sj1);
-            }
+        for (int b0 = 0; b0 < M; b0 += kWcBatch) {
             // home particles still below the cap
             const unsigned todo = __ballot_sync(full, home && cnt < cap);
             if (!todo) break;
+            // Batch candidates q = b0 + 32 u + lane.  Bw[u] bit l: a non-empty
+            // walk voxel starts at q = b0 + 32 u + l (l >= 1 when u = 0); the
+            // rank of the voxel holding q is the number of non-empty voxels
+            // starting at or before b0, minus one, plus the set bits up to q.
+            const int pk = Pk - b0;
+            unsigned Bw[kWcPerLane];
+#pragma unroll
+            for (int u = 0; u < kWcPerLane; ++u)
+                Bw[u] = __reduce_or_sync(
+                    full, (nzk && pk >= 1 && (pk >> 5) == u) ? (1u << (pk & 31)) : 0u);
+            int rank = __popc(__ballot_sync(full, nzk && pk <= 0)) - 1;
+            // past the end of the walk: +inf coordinates, never within h
+            float4 pj[kWcPerLane];
+            int sj[kWcPerLane];
+#pragma unroll
+            for (int u = 0; u < kWcPerLane; ++u) {
+                const int q = b0 + 32 * u + lane;
+                pj[u] = make_float4(inf, inf, inf, 0.f);
+                sj[u] = -1;
+                if (q < M) {
+                    sj[u] = q + S.off[rank + __popc(Bw[u] & le)];
+                    pj[u] = __ldg(pos + sj[u]);
+                }
+                rank += __popc(Bw[u]);
+            }
             // Fast pass: FP32 decisions only.  A pair in the FP32 guard band
             // around h^2 is rare; if any occurs, the whole batch is redone from
             // the counts it started with, deciding those pairs in FP64.  Every
@@ -233,36 +245,38 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             bool band_seen = false;
             for (unsigned t = todo; t; t &= t - 1) {
                 const int i = __ffs(t) - 1;
-                const int ci = __shfl_sync(full, cnt, i);
+                int r = __shfl_sync(full, cnt, i);
                 const float4 ph = S.home[i];
-                const float d20 = dist2(ph, pj0), d21 = dist2(ph, pj1);
-                const bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
-                band_seen |= (!acc0 && d20 <= h2_hi) || (!acc1 && d21 <= h2_hi);
-                const unsigned m0 = __ballot_sync(full, acc0), m1 = __ballot_sync(full, acc1);
-                const int n0 = __popc(m0);
-                const int r0 = ci + __popc(m0 & lt), r1 = ci + n0 + __popc(m1 & lt);
-                if (acc0 && r0 < cap) S.list[i][r0] = sj0;
-                if (acc1 && r1 < cap) S.list[i][r1] = sj1;
-                if (lane == i) cnt = ci + n0 + __popc(m1);
+#pragma unroll
+                for (int u = 0; u < kWcPerLane; ++u) {
+                    const float d2 = dist2(ph, pj[u]);
+                    const bool acc = d2 < h2_lo;
+                    band_seen |= !acc && d2 <= h2_hi;
+                    const unsigned m = __ballot_sync(full, acc);
+                    const int ru = r + __popc(m & lt);
+                    if (acc && ru < cap) S.list[i][ru] = sj[u];
+                    r += __popc(m);
+                }
+                if (lane == i) cnt = r;
             }
             if (__any_sync(full, band_seen)) {
                 cnt = cnt0;
                 for (unsigned t = todo; t; t &= t - 1) {
                     const int i = __ffs(t) - 1;
-                    const int ci = __shfl_sync(full, cnt, i);
+                    int r = __shfl_sync(full, cnt, i);
                     const float4 ph = S.home[i];
-                    const float d20 = dist2(ph, pj0), d21 = dist2(ph, pj1);
-                    bool acc0 = d20 < h2_lo, acc1 = d21 < h2_lo;
-                    if (!acc0 && d20 <= h2_hi)
-                        acc0 = within_exact(ph.x, ph.y, ph.z, pj0.x, pj0.y, pj0.z, h_d);
-                    if (!acc1 && d21 <= h2_hi)
-                        acc1 = within_exact(ph.x, ph.y, ph.z, pj1.x, pj1.y, pj1.z, h_d);
-                    const unsigned m0 = __ballot_sync(full, acc0), m1 = __ballot_sync(full, acc1);
-                    const int n0 = __popc(m0);
-                    const int r0 = ci + __popc(m0 & lt), r1 = ci + n0 + __popc(m1 & lt);
-                    if (acc0 && r0 < cap) S.list[i][r0] = sj0;
-                    if (acc1 && r1 < cap) S.list[i][r1] = sj1;
-                    if (lane == i) cnt = ci + n0 + __popc(m1);
+#pragma unroll
+                    for (int u = 0; u < kWcPerLane; ++u) {
+                        const float d2 = dist2(ph, pj[u]);
+                        bool acc = d2 < h2_lo;
+                        if (!acc && d2 <= h2_hi)
+                            acc = within_exact(ph.x, ph.y, ph.z, pj[u].x, pj[u].y, pj[u].z, h_d);
+                        const unsigned m = __ballot_sync(full, acc);
+                        const int ru = r + __popc(m & lt);
+                        if (acc && ru < cap) S.list[i][ru] = sj[u];
+                        r += __popc(m);
+                    }
+                    if (lane == i) cnt = r;
                 }
             }
         }
