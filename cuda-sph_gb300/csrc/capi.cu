@@ -119,6 +119,10 @@ struct SphgbCtx {
     // streams and graphs
     cudaStream_t cap_stream = nullptr;
     cudaStream_t host_stream = nullptr;
+    // second stream and events of the host-buffer entry point: the velocity
+    // upload and the density download overlap the step's kernels
+    cudaStream_t host_stream2 = nullptr;
+    cudaEvent_t host_ev[5] = {};
     std::map<int, cudaGraphExec_t> graphs;
 
     Launch launch(cudaStream_t st) const {
@@ -162,6 +166,9 @@ void free_ctx(SphgbCtx* c) {
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->host_stream) cudaStreamDestroy(c->host_stream);
+    if (c->host_stream2) cudaStreamDestroy(c->host_stream2);
+    for (cudaEvent_t e : c->host_ev)
+        if (e) cudaEventDestroy(e);
     delete c;
 }
 
@@ -249,10 +256,12 @@ __global__ void k_load_aos(const SceneDev* __restrict__ scenes, const int32_t* _
                            double* __restrict__ pos64_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (vel)
+        vel_out[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
+    if (!pos) return;   // velocities only
     const int si = scene_of(i, pbegin, n_scenes);
     const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
     pos_out[i] = make_float4((float)x, (float)y, (float)z, 0.0f);
-    vel_out[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
     pid_out[i] = i - __ldg(pbegin + si);
     if (pos64_out) {
         // the FP64 accumulator takes the input as given (an exported pipe state
@@ -441,7 +450,8 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const float4* vel,
                      const int32_t* pid, const double* pos64, float4* pos_o, float4* vel_o,
                      int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
-                     cudaEvent_t* ev = nullptr, bool with_tasks = false) {
+                     cudaEvent_t* ev = nullptr, bool with_tasks = false,
+                     cudaEvent_t gather_wait = nullptr) {
     cudaStream_t st = L.stream;
     if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * c->v_total, st));
     SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 2 * sizeof(int32_t), st));
@@ -453,6 +463,8 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                               c->big_count));
     SPHGB_CUDA(launch_sort_big(L, c->big_list, c->big_count, vstart, vcount, c->tmp_pid));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[2], st));
+    // the gather reads the velocities: wait for them when they arrive late
+    if (gather_wait) SPHGB_CUDA(cudaStreamWaitEvent(st, gather_wait, 0));
     SPHGB_CUDA(launch_rank_gather(L, c->cell, c->slot, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
                                   pos_o, vel_o, pid_o, pos64_o, with_tasks ? c->tasks : nullptr,
                                   with_tasks ? c->big_count + 1 : nullptr));
@@ -461,14 +473,18 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
 }
 
 // enqueue one full step on stream st; ev (optional, 8 events): ev[0] at the
-// start and ev[k] after stage k (see SPHGB_PROFILE_STAGES)
-int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+// start and ev[k] after stage k (see SPHGB_PROFILE_STAGES).  gather_wait
+// (optional): an event the rank-gather waits for (velocities uploaded on
+// another stream); density_done (optional): recorded after the density pass.
+int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
+                 cudaEvent_t gather_wait = nullptr, cudaEvent_t density_done = nullptr) {
     const Launch L = c->launch(st);
     double* p64A = c->any_pipe ? c->pos64A : nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
-                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
+                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true,
+                              gather_wait);
     if (rc) return rc;
     if (c->density_variant == SPHGB_DENSITY_WARP)
         SPHGB_CUDA(launch_density_wc(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
@@ -477,6 +493,7 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr) {
         SPHGB_CUDA(launch_density(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
                                   c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
+    if (density_done) SPHGB_CUDA(cudaEventRecord(density_done, st));
     const bool sep = c->out_pos != nullptr;
     SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
                                 c->vcount, c->scene_step, c->nbr, sep ? c->out_pos : c->posA,
@@ -632,6 +649,9 @@ int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes, const double*
     cudaGetDevice(&c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->host_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->host_stream2, cudaStreamNonBlocking);
+    for (cudaEvent_t& ev : c->host_ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         free_ctx(c);
         return cuda_fail(e, "sphgb_ctx_create");
@@ -855,21 +875,57 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
             return fail(SPHGB_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
         }
     }
-    cudaStream_t st = ctx->host_stream;
+    cudaStream_t st = ctx->host_stream, st2 = ctx->host_stream2;
+    cudaEvent_t e_start = ctx->host_ev[0], e_pos = ctx->host_ev[1], e_vel = ctx->host_ev[2],
+                e_rho = ctx->host_ev[3], e_rho_out = ctx->host_ev[4];
     double* sp = ctx->stage;
     double* sv = ctx->stage + 3 * N;
     double* sr = ctx->stage + 6 * N;
-    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-    int rc = sphgb_ctx_load_aos_f64(ctx, sp, sv, st);
+    const size_t b3 = sizeof(double) * 3 * N;
+    const int nb = blocks(ctx->n);
+    // Two streams.  st: position upload, the step, position and velocity
+    // download.  st2: the velocity upload, queued behind the position upload
+    // (they share the host link) so that the hash, scan and scatter passes,
+    // which need positions only, run while it is in flight; then, once the
+    // density pass is done, the density download, which overlaps the force
+    // pass.  Results are the same bits as the one-stream sequence.
+    SPHGB_CUDA(cudaEventRecord(e_start, st));
+    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_start, 0));
+    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, b3, cudaMemcpyHostToDevice, st));
+    SPHGB_CUDA(cudaEventRecord(e_pos, st));
+    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_pos, 0));
+    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, b3, cudaMemcpyHostToDevice, st2));
+    k_load_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                       nullptr, sv, ctx->posA, ctx->velA, ctx->pidA, nullptr);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaEventRecord(e_vel, st2));
+    k_load_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sp,
+                                      nullptr, ctx->posA, ctx->velA, ctx->pidA, ctx->pos64A);
+    SPHGB_CUDA(cudaGetLastError());
+    int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho);
     if (rc) return rc;
-    rc = enqueue_step(ctx, st);
-    if (rc) return rc;
-    rc = sphgb_ctx_store_aos_f64(ctx, sp, sv, sr, st);
-    if (rc) return rc;
-    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    // st2: original index -> slot (from the sorted ids, which the force pass
+    // copies to the output unchanged), then the densities in original order
+    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
+    k_slot_of<<<nb, kBlock, 0, st2>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n, ctx->pidB,
+                                      ctx->slot_of);
+    k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                        nullptr, nullptr, ctx->rho, ctx->slot_of, nullptr,
+                                        nullptr, nullptr, sr);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st2));
+    SPHGB_CUDA(cudaEventRecord(e_rho_out, st2));
+    // st: positions and velocities in original order (slot_of is ready once
+    // the density download has been queued behind it)
+    SPHGB_CUDA(cudaStreamWaitEvent(st, e_rho_out, 0));
+    const bool sep = ctx->out_pos != nullptr;
+    k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                       sep ? ctx->out_pos : ctx->posA,
+                                       sep ? ctx->out_vel : ctx->velA, nullptr, ctx->slot_of,
+                                       sep ? ctx->out_pos64 : ctx->pos64A, sp, sv, nullptr);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, b3, cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, b3, cudaMemcpyDeviceToHost, st));
     SPHGB_CUDA(cudaStreamSynchronize(st));
     return SPHGB_OK;
 }

@@ -100,6 +100,29 @@ def test_host_entry_matches_oracle():
     assert strat.old_state is st and strat.new_state is out and strat.dt == 1 / spec.params.fps
 
 
+@pytest.mark.parametrize("name", ["config0", "pipe"])
+def test_host_entry_bit_identical_to_device_path(name):
+    """Two calls of sphgb_compute_next_state_host in a row (its uploads and
+    downloads spread over two streams) give the same bits as loading the state
+    and stepping it on the device."""
+    torch_cuda()
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()[name]
+    dev = SceneBatch([spec])
+    dev.load_states([st])
+    host = SceneBatch([spec])
+    pos, vel = st.position, st.velocity
+    for _ in range(2):
+        dev.step(1)
+        want = dev.states()[0]
+        pos, vel, rho = host.compute_next_state_host(pos, vel)
+        np.testing.assert_array_equal(pos, want.position)
+        np.testing.assert_array_equal(vel, want.velocity)
+        np.testing.assert_array_equal(rho, want.density)
+    dev.close()
+    host.close()
+
+
 def test_trajectory_config0_200_steps():
     """200 free-running steps of the 8,192-particle dam break against the FP64
     oracle.  The reference's capped walk makes the dynamics chaotic (a pair
