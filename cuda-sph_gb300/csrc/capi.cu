@@ -450,8 +450,7 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const float4* vel,
                      const int32_t* pid, const double* pos64, float4* pos_o, float4* vel_o,
                      int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
-                     cudaEvent_t* ev = nullptr, bool with_tasks = false,
-                     cudaEvent_t gather_wait = nullptr) {
+                     cudaEvent_t* ev = nullptr, bool with_tasks = false) {
     cudaStream_t st = L.stream;
     if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * c->v_total, st));
     SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 2 * sizeof(int32_t), st));
@@ -463,8 +462,6 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                               c->big_count));
     SPHGB_CUDA(launch_sort_big(L, c->big_list, c->big_count, vstart, vcount, c->tmp_pid));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[2], st));
-    // the gather reads the velocities: wait for them when they arrive late
-    if (gather_wait) SPHGB_CUDA(cudaStreamWaitEvent(st, gather_wait, 0));
     SPHGB_CUDA(launch_rank_gather(L, c->cell, c->slot, pid, c->tmp_pid, vstart, vcount, pos, vel, pos64,
                                   pos_o, vel_o, pid_o, pos64_o, with_tasks ? c->tasks : nullptr,
                                   with_tasks ? c->big_count + 1 : nullptr));
@@ -473,27 +470,35 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
 }
 
 // enqueue one full step on stream st; ev (optional, 8 events): ev[0] at the
-// start and ev[k] after stage k (see SPHGB_PROFILE_STAGES).  gather_wait
-// (optional): an event the rank-gather waits for (velocities uploaded on
-// another stream); density_done (optional): recorded after the density pass.
+// start and ev[k] after stage k (see SPHGB_PROFILE_STAGES).  vel_ready
+// (optional): the state in A is in original particle order and its
+// velocities are still being written on another stream; the sort and the
+// density pass go ahead without them and k_gather_vel, after waiting for
+// this event, brings them into slot order for the force pass.  density_done
+// (optional): recorded after the density pass.
 int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                 cudaEvent_t gather_wait = nullptr, cudaEvent_t density_done = nullptr) {
+                 cudaEvent_t vel_ready = nullptr, cudaEvent_t density_done = nullptr) {
     const Launch L = c->launch(st);
     double* p64A = c->any_pipe ? c->pos64A : nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
-    int rc = enqueue_organize(c, L, c->posA, c->velA, c->pidA, p64A, c->posB, c->velB, c->pidB,
-                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true,
-                              gather_wait);
+    const float4* vel_in = vel_ready ? nullptr : c->velA;   // null: gathered after density
+    const float4* vel_s = vel_ready ? nullptr : c->velB;
+    int rc = enqueue_organize(c, L, c->posA, vel_in, c->pidA, p64A, c->posB, c->velB, c->pidB,
+                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
     if (rc) return rc;
     if (c->density_variant == SPHGB_DENSITY_WARP)
-        SPHGB_CUDA(launch_density_wc(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
+        SPHGB_CUDA(launch_density_wc(L, c->posB, vel_s, c->vstart, c->vcount, c->rho, c->fin,
                                      c->nbr, c->tasks, c->big_count + 1));
     else
-        SPHGB_CUDA(launch_density(L, c->posB, c->velB, c->vstart, c->vcount, c->rho, c->fin,
+        SPHGB_CUDA(launch_density(L, c->posB, vel_s, c->vstart, c->vcount, c->rho, c->fin,
                                   c->nbr));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[5], st));
     if (density_done) SPHGB_CUDA(cudaEventRecord(density_done, st));
+    if (vel_ready) {
+        SPHGB_CUDA(cudaStreamWaitEvent(st, vel_ready, 0));
+        SPHGB_CUDA(launch_gather_vel(L, c->pidB, c->velA, c->rho, c->velB, c->fin));
+    }
     const bool sep = c->out_pos != nullptr;
     SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
                                 c->vcount, c->scene_step, c->nbr, sep ? c->out_pos : c->posA,
@@ -885,8 +890,9 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     const int nb = blocks(ctx->n);
     // Two streams.  st: position upload, the step, position and velocity
     // download.  st2: the velocity upload, queued behind the position upload
-    // (they share the host link) so that the hash, scan and scatter passes,
-    // which need positions only, run while it is in flight; then, once the
+    // (they share the host link) so that the voxel sort and the density pass,
+    // which need positions only, run while it is in flight (the step gathers
+    // the velocities into slot order after the density pass); then, once the
     // density pass is done, the density download, which overlaps the force
     // pass.  Results are the same bits as the one-stream sequence.
     SPHGB_CUDA(cudaEventRecord(e_start, st));

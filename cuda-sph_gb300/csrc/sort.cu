@@ -263,7 +263,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
     if (tasks && (r & 31) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
     pid_out[d] = p;
     pos_out[d] = __ldg(pos + s);
-    vel_out[d] = __ldg(vel + s);
+    if (vel) vel_out[d] = __ldg(vel + s);   // null: velocities gathered later
     if (pos64) {
         pos64_out[3 * d + 0] = pos64[3 * s + 0];
         pos64_out[3 * d + 1] = pos64[3 * s + 1];

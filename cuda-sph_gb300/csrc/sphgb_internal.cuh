@@ -410,6 +410,8 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
                               const int32_t* task_count);
+cudaError_t launch_gather_vel(const Launch& L, const int32_t* pid, const float4* vel_in,
+                              const float* rho, float4* vel_out, float4* fin);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
                           const float* rho, const float4* fin, const int32_t* vstart,
                           const int32_t* vcount, float4* pressure, float4* viscosity);

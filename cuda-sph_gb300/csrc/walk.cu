@@ -27,14 +27,17 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // than kListCap (the force pass then walks again).
 // Force inputs of particle s: fin[2s] = (x, y, z, p/rho^2), fin[2s + 1] =
 // (vx, vy, vz, 1/rho), one 32-byte record that the force pass reads per
-// neighbour instead of three separate arrays.
+// neighbour instead of three separate arrays.  With vel null only the first
+// half is written; k_gather_vel writes the second once the velocities are in.
 __device__ __forceinline__ void write_force_inputs(int s, const float4& pi, const SceneDev& sc,
                                                    const float4* __restrict__ vel, float r,
                                                    float4* __restrict__ fin) {
     const float p = sc.k * (r - sc.rho0);
-    const float4 v = __ldg(vel + s);
     fin[2 * s] = make_float4(pi.x, pi.y, pi.z, p / (r * r));
-    fin[2 * s + 1] = make_float4(v.x, v.y, v.z, 1.0f / r);
+    if (vel) {
+        const float4 v = __ldg(vel + s);
+        fin[2 * s + 1] = make_float4(v.x, v.y, v.z, 1.0f / r);
+    }
 }
 
 // One particle's density by a thread-private walk: the walk records neighbour
@@ -322,6 +325,22 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         }
         __syncwarp();
     }
+}
+
+// Velocities of a state loaded in original particle order (scene offset + id)
+// into sorted slot order, with the second half of the force inputs: used when
+// the velocities arrive after the rank-gather (the host-buffer entry point
+// uploads them while the sort and the density pass run).
+__global__ void __launch_bounds__(kBlock)
+k_gather_vel(const int32_t* __restrict__ pbegin, int n_scenes, int n,
+             const int32_t* __restrict__ pid, const float4* __restrict__ vel_in,
+             const float* __restrict__ rho, float4* __restrict__ vel_out,
+             float4* __restrict__ fin) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const float4 v = __ldg(vel_in + __ldg(pbegin + scene_of(d, pbegin, n_scenes)) + __ldg(pid + d));
+    vel_out[d] = v;
+    fin[2 * d + 1] = make_float4(v.x, v.y, v.z, 1.0f / __ldg(rho + d));
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -614,6 +633,14 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
     k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
                                                          vel, vstart, vcount, rho, fin, nbr, tasks,
                                                          task_count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_vel(const Launch& L, const int32_t* pid, const float4* vel_in,
+                              const float* rho, float4* vel_out, float4* fin) {
+    if (L.n == 0) return cudaSuccess;
+    k_gather_vel<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.pbegin, L.n_scenes, L.n, pid, vel_in,
+                                                            rho, vel_out, fin);
     return cudaGetLastError();
 }
 
