@@ -8,6 +8,7 @@
 // which is VoxelSPHStrategy.compute_next_state (sim/src/sph/strategies/
 // abstract_sph_strategy.py:31-46, voxel_sph_strategy.py:20-116) without any
 // host round trip.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -52,6 +53,13 @@ struct ConsChunk {
 };
 
 }  // namespace
+
+// host-buffer entry point: particle-order ranges of the force pass, and its events
+// (start, positions in, velocities in, density done, slot map ready, downloads
+// queued, then one per range)
+constexpr int kHostRanges = 8;
+constexpr int kHostFirstRangeEvent = 6;
+constexpr int kHostEvents = kHostFirstRangeEvent + kHostRanges;
 
 struct SphgbCtx {
     int device = 0;
@@ -122,7 +130,11 @@ struct SphgbCtx {
     // second stream and events of the host-buffer entry point: the velocity
     // upload and the density download overlap the step's kernels
     cudaStream_t host_stream2 = nullptr;
-    cudaEvent_t host_ev[5] = {};
+    cudaEvent_t host_ev[kHostEvents] = {};
+    // force-pass order of the host-buffer entry point (sphgb_ctx_set_host_order)
+    int host_order = SPHGB_HOST_ORDER_AUTO;
+    int host_calls = 0;         // calls since the order was last set
+    double host_ms[3] = {};     // timed call per order (index = order)
     std::map<int, cudaGraphExec_t> graphs;
 
     Launch launch(cudaStream_t st) const {
@@ -469,6 +481,27 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
     return SPHGB_OK;
 }
 
+// force + integrate + wall pass of the step (after the density pass), over
+// all slots, or over a range of particles in original order when range is
+// given (see PidRange)
+int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range) {
+    const bool sep = c->out_pos != nullptr;
+    double* p64B = c->any_pipe ? c->pos64B : nullptr;
+    float4* pos_o = sep ? c->out_pos : c->posA;
+    float4* vel_o = sep ? c->out_vel : c->velA;
+    int32_t* pid_o = sep ? c->out_pid : c->pidA;
+    double* p64_o = c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr;
+    if (range)
+        SPHGB_CUDA(launch_integrate_range(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B,
+                                          c->vstart, c->vcount, c->scene_step, c->nbr, pos_o,
+                                          vel_o, pid_o, p64_o, *range));
+    else
+        SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
+                                    c->vcount, c->scene_step, c->nbr, pos_o, vel_o, pid_o, p64_o,
+                                    nullptr));
+    return SPHGB_OK;
+}
+
 // enqueue one full step on stream st; ev (optional, 8 events): ev[0] at the
 // start and ev[k] after stage k (see SPHGB_PROFILE_STAGES).  vel_ready
 // (optional): the state in A is in original particle order and its
@@ -476,8 +509,11 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
 // density pass go ahead without them and k_gather_vel, after waiting for
 // this event, brings them into slot order for the force pass.  density_done
 // (optional): recorded after the density pass.
+// with_forces = false stops after the density pass (and the velocity gather):
+// the caller then runs enqueue_forces itself and the step counter.
 int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
-                 cudaEvent_t vel_ready = nullptr, cudaEvent_t density_done = nullptr) {
+                 cudaEvent_t vel_ready = nullptr, cudaEvent_t density_done = nullptr,
+                 bool with_forces = true) {
     const Launch L = c->launch(st);
     double* p64A = c->any_pipe ? c->pos64A : nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
@@ -499,12 +535,9 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
         SPHGB_CUDA(cudaStreamWaitEvent(st, vel_ready, 0));
         SPHGB_CUDA(launch_gather_vel(L, c->pidB, c->velA, c->rho, c->velB, c->fin));
     }
-    const bool sep = c->out_pos != nullptr;
-    SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
-                                c->vcount, c->scene_step, c->nbr, sep ? c->out_pos : c->posA,
-                                sep ? c->out_vel : c->velA, sep ? c->out_pid : c->pidA,
-                                c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr,
-                                nullptr));
+    if (!with_forces) return SPHGB_OK;
+    rc = enqueue_forces(c, L, nullptr);
+    if (rc) return rc;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[6], st));
     k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
     SPHGB_CUDA(cudaGetLastError());
@@ -844,6 +877,19 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
     return rc;
 }
 
+namespace {
+// Force-pass order of the next host-entry call.  AUTO: call 1 (allocations,
+// first touches) and call 2 run in slot order, call 3 in particle order; calls 2
+// and 3 are timed, and later calls take the faster order.
+int host_order_for_call(const SphgbCtx* c) {
+    if (c->host_order != SPHGB_HOST_ORDER_AUTO) return c->host_order;
+    if (c->host_calls < 2) return SPHGB_HOST_ORDER_SLOT;
+    if (c->host_calls == 2) return SPHGB_HOST_ORDER_PARTICLE;
+    return c->host_ms[SPHGB_HOST_ORDER_PARTICLE] < c->host_ms[SPHGB_HOST_ORDER_SLOT]
+               ? SPHGB_HOST_ORDER_PARTICLE : SPHGB_HOST_ORDER_SLOT;
+}
+}  // namespace
+
 int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
                                   double* h_pos_out, double* h_vel_out, double* h_rho_out) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
@@ -882,7 +928,7 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     }
     cudaStream_t st = ctx->host_stream, st2 = ctx->host_stream2;
     cudaEvent_t e_start = ctx->host_ev[0], e_pos = ctx->host_ev[1], e_vel = ctx->host_ev[2],
-                e_rho = ctx->host_ev[3], e_rho_out = ctx->host_ev[4];
+                e_rho = ctx->host_ev[3], e_slot = ctx->host_ev[4], e_done = ctx->host_ev[5];
     double* sp = ctx->stage;
     double* sv = ctx->stage + 3 * N;
     double* sr = ctx->stage + 6 * N;
@@ -908,31 +954,77 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     k_load_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sp,
                                       nullptr, ctx->posA, ctx->velA, ctx->pidA, ctx->pos64A);
     SPHGB_CUDA(cudaGetLastError());
-    int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho);
+    const int order = host_order_for_call(ctx);
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho, order == SPHGB_HOST_ORDER_SLOT);
     if (rc) return rc;
     // st2: original index -> slot (from the sorted ids, which the force pass
     // copies to the output unchanged), then the densities in original order
     SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
     k_slot_of<<<nb, kBlock, 0, st2>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n, ctx->pidB,
                                       ctx->slot_of);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaEventRecord(e_slot, st2));
     k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                         nullptr, nullptr, ctx->rho, ctx->slot_of, nullptr,
                                         nullptr, nullptr, sr);
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaMemcpyAsync(h_rho_out, sr, sizeof(double) * N, cudaMemcpyDeviceToHost, st2));
-    SPHGB_CUDA(cudaEventRecord(e_rho_out, st2));
-    // st: positions and velocities in original order (slot_of is ready once
-    // the density download has been queued behind it)
-    SPHGB_CUDA(cudaStreamWaitEvent(st, e_rho_out, 0));
-    const bool sep = ctx->out_pos != nullptr;
-    k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
-                                       sep ? ctx->out_pos : ctx->posA,
-                                       sep ? ctx->out_vel : ctx->velA, nullptr, ctx->slot_of,
-                                       sep ? ctx->out_pos64 : ctx->pos64A, sp, sv, nullptr);
-    SPHGB_CUDA(cudaGetLastError());
-    SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, b3, cudaMemcpyDeviceToHost, st));
-    SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, b3, cudaMemcpyDeviceToHost, st));
+    if (order == SPHGB_HOST_ORDER_SLOT) {
+        // st: positions and velocities in original order once the step is
+        // done and the slot map is ready, then downloaded whole
+        SPHGB_CUDA(cudaEventRecord(e_done, st2));
+        SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
+        const bool sep = ctx->out_pos != nullptr;
+        k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                           sep ? ctx->out_pos : ctx->posA,
+                                           sep ? ctx->out_vel : ctx->velA, nullptr, ctx->slot_of,
+                                           sep ? ctx->out_pos64 : ctx->pos64A, sp, sv, nullptr);
+        SPHGB_CUDA(cudaGetLastError());
+        SPHGB_CUDA(cudaMemcpyAsync(h_pos_out, sp, b3, cudaMemcpyDeviceToHost, st));
+        SPHGB_CUDA(cudaMemcpyAsync(h_vel_out, sv, b3, cudaMemcpyDeviceToHost, st));
+    } else {
+        // st: the force pass in original particle order, kHostRanges ranges;
+        // st2 downloads each range's rows while st computes the next
+        SPHGB_CUDA(cudaStreamWaitEvent(st, e_slot, 0));
+        const Launch L = ctx->launch(st);
+        for (int r = 0; r < kHostRanges; ++r) {
+            PidRange range;
+            range.slot_of = ctx->slot_of;
+            range.i0 = (int)(N * r / kHostRanges);
+            range.i1 = (int)(N * (r + 1) / kHostRanges);
+            range.pos = sp;
+            range.vel = sv;
+            rc = enqueue_forces(ctx, L, &range);
+            if (rc) return rc;
+            SPHGB_CUDA(cudaEventRecord(ctx->host_ev[kHostFirstRangeEvent + r], st));
+            SPHGB_CUDA(cudaStreamWaitEvent(st2, ctx->host_ev[kHostFirstRangeEvent + r], 0));
+            const size_t off = 3 * (size_t)range.i0, len = sizeof(double) * 3 * (range.i1 - range.i0);
+            SPHGB_CUDA(cudaMemcpyAsync(h_pos_out + off, sp + off, len, cudaMemcpyDeviceToHost, st2));
+            SPHGB_CUDA(cudaMemcpyAsync(h_vel_out + off, sv + off, len, cudaMemcpyDeviceToHost, st2));
+        }
+        k_step_counter<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->scene_step, ctx->n_scenes);
+        SPHGB_CUDA(cudaGetLastError());
+        SPHGB_CUDA(cudaEventRecord(e_done, st2));
+        SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
+    }
     SPHGB_CUDA(cudaStreamSynchronize(st));
+    const double ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (ctx->host_calls < 1000) ++ctx->host_calls;
+    if (ctx->host_order == SPHGB_HOST_ORDER_AUTO && ctx->host_calls >= 2 && ctx->host_calls <= 3)
+        ctx->host_ms[order] = ms;   // calls 2 and 3 time the two orders (call 1 warms up)
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_set_host_order(SphgbCtx* ctx, int order) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (order != SPHGB_HOST_ORDER_AUTO && order != SPHGB_HOST_ORDER_SLOT &&
+        order != SPHGB_HOST_ORDER_PARTICLE)
+        return fail(SPHGB_ERR_INVALID, "order must be SPHGB_HOST_ORDER_AUTO, _SLOT or _PARTICLE");
+    ctx->host_order = order;
+    ctx->host_calls = 0;
+    ctx->host_ms[1] = ctx->host_ms[2] = 0.0;
     return SPHGB_OK;
 }
 

@@ -362,6 +362,17 @@ struct NbrList {
     int32_t* count = nullptr;   // n entries; -1 = more than kListCap neighbours
 };
 
+// Force pass over a range of particles in original order (scene offset +
+// particle id): particle i is at slot slot_of[i], and its next position and
+// velocity are also written as FP64 rows i of pos / vel (the host-buffer
+// entry point downloads each range while the next one is computed).
+struct PidRange {
+    const int32_t* slot_of = nullptr;
+    int i0 = 0, i1 = 0;
+    double* pos = nullptr;      // (n, 3) FP64
+    double* vel = nullptr;      // (n, 3) FP64
+};
+
 // ---- launchers (host) -----------------------------------------------------
 struct Launch {
     const SceneDev* scenes;     // device array
@@ -421,6 +432,12 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
                              float4* force_out);
+cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const float4* vel,
+                                   const float* rho, const float4* fin, const int32_t* pid,
+                                   const double* pos64, const int32_t* vstart,
+                                   const int32_t* vcount, const int32_t* scene_step, NbrList nbr,
+                                   float4* pos_out, float4* vel_out, int32_t* pid_out,
+                                   double* pos64_out, PidRange range);
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, int32_t* list, int stride,
                               int32_t* n_capped, int32_t* n_uncapped);

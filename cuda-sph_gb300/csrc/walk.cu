@@ -518,8 +518,11 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
 // (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
 // state into the *_out buffers at the same slot.  kPipe = false is the
-// instantiation for contexts without pipe scenes (no FP64 code).
-template <bool kPipe>
+// instantiation for contexts without pipe scenes (no FP64 code).  kRange:
+// one thread per particle of range.i0..i1 in original order (same per-particle
+// arithmetic), which also writes the FP64 rows of the next position and
+// velocity.
+template <bool kPipe, bool kRange>
 __global__ void __launch_bounds__(kBlock, kPipe ? 1 : 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
@@ -529,9 +532,16 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
             NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
-            float4* __restrict__ force_out) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+            float4* __restrict__ force_out, PidRange range) {
+    int s, row = 0;
+    if (kRange) {
+        row = range.i0 + blockIdx.x * blockDim.x + threadIdx.x;
+        if (row >= range.i1) return;
+        s = __ldg(range.slot_of + row);
+    } else {
+        s = blockIdx.x * blockDim.x + threadIdx.x;
+        if (s >= n) return;
+    }
     const int si = scene_of(s, pbegin, n_scenes);
     const SceneDev& sc = scenes[si];
     const float4 pi = __ldg(pos + s);
@@ -566,6 +576,11 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             pos64_out[3 * s + 1] = x[1];
             pos64_out[3 * s + 2] = x[2];
         }
+        if (kRange) {
+            range.pos[3 * (size_t)row + 0] = x[0];
+            range.pos[3 * (size_t)row + 1] = x[1];
+            range.pos[3 * (size_t)row + 2] = x[2];
+        }
     } else if (kPipe) {
         // pipe flow: FP64 position accumulator and FP64 wall response
         double x[3], vd[3];
@@ -580,10 +595,16 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
         for (int a = 0; a < 3; ++a) {
             v[a] = (float)vd[a];
             pos64_out[3 * s + a] = x[a];
+            if (kRange) range.pos[3 * (size_t)row + a] = x[a];
         }
         pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
     }
     vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
+    if (kRange) {
+        range.vel[3 * (size_t)row + 0] = v[0];
+        range.vel[3 * (size_t)row + 1] = v[1];
+        range.vel[3 * (size_t)row + 2] = v[2];
+    }
     pid_out[s] = p_id;
     if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
 }
@@ -671,13 +692,34 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
                              float4* force_out) {
     if (L.n == 0) return cudaSuccess;
     if (L.pipe_scenes)
-        k_integrate<true><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
+        k_integrate<true, false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, PidRange{});
     else
-        k_integrate<false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
+        k_integrate<false, false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out);
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, PidRange{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const float4* vel,
+                                   const float* rho, const float4* fin, const int32_t* pid,
+                                   const double* pos64, const int32_t* vstart,
+                                   const int32_t* vcount, const int32_t* scene_step, NbrList nbr,
+                                   float4* pos_out, float4* vel_out, int32_t* pid_out,
+                                   double* pos64_out, PidRange range) {
+    const int m = range.i1 - range.i0;
+    if (m <= 0) return cudaSuccess;
+    if (range.i0 < 0 || range.i1 > L.n || !range.slot_of || !range.pos || !range.vel)
+        return cudaErrorInvalidValue;
+    if (L.pipe_scenes)
+        k_integrate<true, true><<<blocks_for(m), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, nullptr, range);
+    else
+        k_integrate<false, true><<<blocks_for(m), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, nullptr, range);
     return cudaGetLastError();
 }
 

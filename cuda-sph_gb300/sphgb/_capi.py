@@ -14,6 +14,7 @@ from . import _build
 MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
 DENSITY_WARP, DENSITY_THREAD = 0, 1
+HOST_ORDER_AUTO, HOST_ORDER_SLOT, HOST_ORDER_PARTICLE = 0, 1, 2
 
 ERRORS = {
     -1: "SPHGB_ERR_INVALID",
@@ -94,6 +95,7 @@ SIGNATURES = [
     ("sphgb_ctx_step", _I, [_VP, _I, _I, _VP]),
     ("sphgb_ctx_step_profiled", _I, [_VP, _I, _VP, C.POINTER(C.c_float)]),
     ("sphgb_compute_next_state_host", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    ("sphgb_ctx_set_host_order", _I, [_VP, _I]),
     ("sphgb_ctx_conservation", _I, [_VP, _VP, _VP]),
     ("sphgb_ctx_neighbour_counts", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_assign_voxels", _I, [_VP, _VP, _VP, _VP]),

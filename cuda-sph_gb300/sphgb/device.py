@@ -138,6 +138,11 @@ class SceneBatch:
         _capi.call("sphgb_ctx_set_tuning", self._ctx, int(sort_block), int(density_variant),
                    int(big_voxel))
 
+    def set_host_order(self, order: int = _capi.HOST_ORDER_AUTO) -> None:
+        """Force-pass order of compute_next_state_host; results are unchanged
+        (see sphgb_ctx_set_host_order)."""
+        _capi.call("sphgb_ctx_set_host_order", self._ctx, int(order))
+
     # -- helpers ---------------------------------------------------------
     def _stream(self, stream=None) -> int:
         torch = self._torch

@@ -166,6 +166,16 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
  * through device staging buffers. */
 int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
                                   double* h_pos_out, double* h_vel_out, double* h_rho_out);
+/* Order in which sphgb_compute_next_state_host runs its force pass (results
+ * do not change).  SPHGB_HOST_ORDER_SLOT: voxel-sorted order, then the next
+ * state is downloaded whole.  SPHGB_HOST_ORDER_PARTICLE: original particle
+ * order in ranges, each range's rows downloaded while the next range is
+ * computed; faster when nearby particle ids are nearby in space, slower when
+ * they are scattered.  SPHGB_HOST_ORDER_AUTO (default): the first calls time
+ * both orders and later calls take the faster.  No counterpart in the
+ * reference (its step is synchronous, abstract_sph_strategy.py:31-46). */
+enum { SPHGB_HOST_ORDER_AUTO = 0, SPHGB_HOST_ORDER_SLOT = 1, SPHGB_HOST_ORDER_PARTICLE = 2 };
+int sphgb_ctx_set_host_order(SphgbCtx* ctx, int order);
 
 /* Per-scene conservation sums in FP64, fixed summation order (identical for a
  * scene whether it runs alone or batched).  d_out: 8 doubles per scene:

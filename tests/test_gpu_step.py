@@ -100,19 +100,24 @@ def test_host_entry_matches_oracle():
     assert strat.old_state is st and strat.new_state is out and strat.dt == 1 / spec.params.fps
 
 
+@pytest.mark.parametrize("order", ["slot", "particle", "auto"])
 @pytest.mark.parametrize("name", ["config0", "pipe"])
-def test_host_entry_bit_identical_to_device_path(name):
-    """Two calls of sphgb_compute_next_state_host in a row (its uploads and
-    downloads spread over two streams) give the same bits as loading the state
+def test_host_entry_bit_identical_to_device_path(name, order):
+    """Calls of sphgb_compute_next_state_host in a row (uploads and downloads
+    spread over two streams; the force pass in slot order, in particle-order
+    ranges, or chosen by timing both) give the same bits as loading the state
     and stepping it on the device."""
     torch_cuda()
+    from sphgb import _capi
     from sphgb.device import SceneBatch
     spec, st = _scenes()[name]
     dev = SceneBatch([spec])
     dev.load_states([st])
     host = SceneBatch([spec])
+    host.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE,
+                         "auto": _capi.HOST_ORDER_AUTO}[order])
     pos, vel = st.position, st.velocity
-    for _ in range(2):
+    for _ in range(5 if order == "auto" else 2):   # auto: warm-up, both timed orders, choice
         dev.step(1)
         want = dev.states()[0]
         pos, vel, rho = host.compute_next_state_host(pos, vel)
