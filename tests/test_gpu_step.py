@@ -128,6 +128,26 @@ def test_host_entry_bit_identical_to_device_path(name, order):
     host.close()
 
 
+@pytest.mark.parametrize("shape", [(3, 7, 5), (1, 5, 1)])
+def test_host_entry_particle_ranges_uneven_counts(shape):
+    """Particle-order ranges when the particle count does not split evenly
+    into the ranges (105 particles), or is below their number (5 particles:
+    some ranges empty): same bits as the slot-order call."""
+    torch_cuda()
+    from sphgb import _capi, scenes
+    from sphgb.device import SceneBatch
+    nx, ny, nz = shape
+    spec, st = scenes.box_dam_break(nx=nx, ny=ny, nz=nz, seed=21)
+    outs = []
+    for order in (_capi.HOST_ORDER_SLOT, _capi.HOST_ORDER_PARTICLE):
+        b = SceneBatch([spec])
+        b.set_host_order(order)
+        outs.append(b.compute_next_state_host(st.position, st.velocity))
+        b.close()
+    for a, c in zip(*outs):
+        np.testing.assert_array_equal(a, c)
+
+
 def test_trajectory_config0_200_steps():
     """200 free-running steps of the 8,192-particle dam break against the FP64
     oracle.  The reference's capped walk makes the dynamics chaotic (a pair
