@@ -22,7 +22,10 @@ single scene does not shard; replicas only).  Also reported:
            (sphgb_compute_next_state_host): FP64 AoS state copied from pinned
            host memory and the next state copied back, every step;
   roofline the dominant kernel's algorithmic bytes / its mean CUDA-event time;
-  cpu_baseline  the oracle's C/OpenMP FP64 step on the host cores (rank 0).
+  cpu_baseline  the oracle's C/OpenMP FP64 step on the host cores (rank 0);
+  oracle_err    the step's error against that FP64 step of the same input;
+  batched, served, pipe_flow  the batched-scene, served-request and pipe-flow
+           workloads (skipped with --no-batched).
 --impl reference: the reference's algorithm on the host cores (the oracle's
 C/OpenMP restatement; the reference itself is numba-CUDA Python and cannot run
 here), same metric; rank 0 only.
@@ -221,11 +224,25 @@ def cpu_baseline(spec, state, steps):
     # like the timed GPU steps: every step is a full step of the step-0 state
     t0 = time.perf_counter()
     for _ in range(steps):
-        ref.step(sp, pos, vel, step_index=0)
+        out = ref.step(sp, pos, vel, step_index=0)
     dt = time.perf_counter() - t0
     return {"value": spec.n * steps / dt, "unit": "particle-steps/s", "cores": ref.num_threads(),
             "kind": "port", "sample": f"{steps} full steps of the {spec.n}-particle scene's step-0 "
-                                     f"state ({dt:.1f} s wall, FP64 C/OpenMP restatement)"}
+                                     f"state ({dt:.1f} s wall, FP64 C/OpenMP restatement)"}, out
+
+
+def oracle_error(got, want):
+    """The GPU step against the FP64 oracle's step of the same input: density
+    relative error, position absolute error, and velocity error over the
+    largest velocity (cancellation in the force sum makes a per-particle
+    relative velocity error meaningless)."""
+    import numpy as np
+    (gp, gv, gr), (wp, wv, wr) = got, want
+    ok = np.isfinite(wr) & (wr > 0)
+    return {"density_max_rel": float(np.max(np.abs(gr[ok] - wr[ok]) / wr[ok])),
+            "position_max_abs": float(np.max(np.abs(gp - wp))),
+            "velocity_max_abs_over_max": float(np.max(np.abs(gv - wv)) / np.max(np.abs(wv))),
+            "particles_compared": int(ok.sum())}
 
 
 def run_gb300(args):
@@ -348,12 +365,16 @@ def run_gb300(args):
                         "ms_per_step": summary(tried)},
            "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(spec, state, args.cpu_steps)
+        out["cpu_baseline"], want = cpu_baseline(spec, state, max(args.cpu_steps, 1))
         log(f"cpu baseline: {out['cpu_baseline']}")
+        # the end-to-end outputs are one step of the same step-0 state
+        out["oracle_err"] = oracle_error((o_pos, o_vel, o_rho), want)
+        log(f"error against the FP64 oracle: {out['oracle_err']}")
     batch.close()
     if not args.no_batched and args.workload == "config2":
         out["batched"] = batched_section(args)
         out["served"] = served_section(args)
+        out["pipe_flow"] = pipe_section(args)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -391,6 +412,38 @@ def batched_section(args):
             "vs_plain": tb and tp / tb, "vs_plain_graph": tg / tb,
             "identical_to_plain": bool(same), "density_rel_err_vs_fp64": err,
             "graph": "all scenes and steps in one CUDA graph launch"}
+
+
+def pipe_section(args):
+    """Pipe flow (262,144 particles in the 3-segment pipe, FP64 position
+    accumulator and pipe wall response with respawns): the 1,000 steps of the
+    workload, free-running from the generated start state, 10 steps per
+    graph launch, CUDA events around all of them."""
+    import torch
+    from sphgb import scenes
+    from sphgb.device import SceneBatch
+    spec, st = scenes.config1()
+    b = SceneBatch([spec])
+    b.load_states([st])
+    b.step(10, use_graph=True)      # captures the 10-step graph
+    b.load_states([st])             # back to the start state and step 0
+    torch.cuda.synchronize()
+    steps = 1000
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps // 10):
+        b.step(10, use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    nonfinite = int((~torch.isfinite(b.pos[:, :3]).all(dim=1)).sum())
+    cons = b.conservation()[0]
+    b.close()
+    log(f"pipe flow: {spec.n} particles x {steps} steps in {ms:.1f} ms")
+    return {"particles": spec.n, "steps": steps, "value": spec.n * steps / (ms / 1e3),
+            "unit": "particle-steps/s", "ms_per_step": ms / steps,
+            "nonfinite_particles": nonfinite, "mass_fp64": float(cons[0]),
+            "graph": "10 steps per CUDA graph launch"}
 
 
 def served_section(args):

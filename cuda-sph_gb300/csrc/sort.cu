@@ -271,8 +271,6 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
     }
 }
 
-inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
-
 }  // namespace
 
 int scan_tiles(int v_total) { return (v_total + kScanTile - 1) / kScanTile; }

@@ -137,12 +137,135 @@ constexpr int kSelfTerm = 0x7fc0dead;
 constexpr int kWcList = kListCap;       // accepted neighbours per particle, self included
 constexpr int kWcPerLane = 3;           // candidates per lane in one batch
 constexpr int kWcBatch = 32 * kWcPerLane;
+constexpr int kWcCullMin = 4 * kWcBatch;  // walks longer than this skip unreachable batches
+
+// Bit k (k = 9 (dx + 1) + 3 (dy + 1) + dz + 1, the walk order) is set when walk
+// voxel k of voxel (vx, vy, vz) may hold a particle within h of p: the same
+// box-distance test as walk() in sphgb_internal.cuh, against the widened
+// bound cull2.
+__device__ __forceinline__ unsigned reach_mask(const float4& p, int vx, int vy, int vz,
+                                               const SceneDev& sc) {
+    const float fx = p.x - (float)vx * sc.vs[0];
+    const float fy = p.y - (float)vy * sc.vs[1];
+    const float fz = p.z - (float)vz * sc.vs[2];
+    const float gx[3] = {fx * fx, 0.0f, (sc.vs[0] - fx) * (sc.vs[0] - fx)};
+    const float gy[3] = {fy * fy, 0.0f, (sc.vs[1] - fy) * (sc.vs[1] - fy)};
+    const float gz[3] = {fz * fz, 0.0f, (sc.vs[2] - fz) * (sc.vs[2] - fz)};
+    unsigned m = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float gxy = gx[a] + gy[b];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (!(gxy + gz[c] > sc.cull2)) m |= 1u << (9 * a + 3 * b + c);
+        }
+    return m;
+}
 
 struct WcShared {
     float4 home[32];
     int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
     int32_t off[27];    // first slot - first walk index of each non-empty walk voxel, by rank
 };
+
+// The candidate loop of k_density_wc for one task: batches of kWcBatch
+// candidates in walk order, each tested against every home particle still
+// below the cap.  Accepted slots go to S.list[i] in walk order and the counts
+// to cnt (lane i: home particle i).  Lane k < 27 holds walk voxel k's first
+// walk index Pk and member count ck.  kCull: a home particle skips the batches
+// that lie wholly in walk voxels outside its reach mask.
+template <bool kCull>
+__device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, int cap, int M,
+                                              int Pk, int ck, bool nzk, unsigned reach,
+                                              const float4* __restrict__ pos, float h2_lo,
+                                              float h2_hi, double h_d) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned le = (2u << lane) - 1u;      // bits 0..lane
+    const float inf = __int_as_float(0x7f800000);
+    for (int b0 = 0; b0 < M; b0 += kWcBatch) {
+        // home particles still below the cap
+        unsigned todo = __ballot_sync(full, home && cnt < cap);
+        if (!todo) break;
+        if (kCull) {
+            // walk voxels overlapping this batch, and the homes that reach one
+            const unsigned span =
+                __ballot_sync(full, nzk && Pk < b0 + kWcBatch && Pk + ck > b0);
+            todo &= __ballot_sync(full, (reach & span) != 0u);
+            if (!todo) continue;
+        }
+        // Batch candidates q = b0 + 32 u + lane.  Bw[u] bit l: a non-empty
+        // walk voxel starts at q = b0 + 32 u + l (l >= 1 when u = 0); the
+        // rank of the voxel holding q is the number of non-empty voxels
+        // starting at or before b0, minus one, plus the set bits up to q.
+        const int pk = Pk - b0;
+        unsigned Bw[kWcPerLane];
+#pragma unroll
+        for (int u = 0; u < kWcPerLane; ++u)
+            Bw[u] = __reduce_or_sync(
+                full, (nzk && pk >= 1 && (pk >> 5) == u) ? (1u << (pk & 31)) : 0u);
+        int rank = __popc(__ballot_sync(full, nzk && pk <= 0)) - 1;
+        // past the end of the walk: +inf coordinates, never within h
+        float4 pj[kWcPerLane];
+        int sj[kWcPerLane];
+#pragma unroll
+        for (int u = 0; u < kWcPerLane; ++u) {
+            const int q = b0 + 32 * u + lane;
+            pj[u] = make_float4(inf, inf, inf, 0.f);
+            sj[u] = -1;
+            if (q < M) {
+                sj[u] = q + S.off[rank + __popc(Bw[u] & le)];
+                pj[u] = __ldg(pos + sj[u]);
+            }
+            rank += __popc(Bw[u]);
+        }
+        // Fast pass: FP32 decisions only.  A pair in the FP32 guard band
+        // around h^2 is rare; if any occurs, the whole batch is redone from
+        // the counts it started with, deciding those pairs in FP64.  Every
+        // list entry below the final counts is rewritten by the redo.
+        const int cnt0 = cnt;
+        bool band_seen = false;
+        for (unsigned t = todo; t; t &= t - 1) {
+            const int i = __ffs(t) - 1;
+            int r = __shfl_sync(full, cnt, i);
+            const float4 ph = S.home[i];
+#pragma unroll
+            for (int u = 0; u < kWcPerLane; ++u) {
+                const float d2 = dist2(ph, pj[u]);
+                const bool acc = d2 < h2_lo;
+                band_seen |= !acc && d2 <= h2_hi;
+                const unsigned m = __ballot_sync(full, acc);
+                const int ru = r + __popc(m & lt);
+                if (acc && ru < cap) S.list[i][ru] = sj[u];
+                r += __popc(m);
+            }
+            if (lane == i) cnt = r;
+        }
+        if (__any_sync(full, band_seen)) {
+            cnt = cnt0;
+            for (unsigned t = todo; t; t &= t - 1) {
+                const int i = __ffs(t) - 1;
+                int r = __shfl_sync(full, cnt, i);
+                const float4 ph = S.home[i];
+#pragma unroll
+                for (int u = 0; u < kWcPerLane; ++u) {
+                    const float d2 = dist2(ph, pj[u]);
+                    bool acc = d2 < h2_lo;
+                    if (!acc && d2 <= h2_hi)
+                        acc = within_exact(ph.x, ph.y, ph.z, pj[u].x, pj[u].y, pj[u].z, h_d);
+                    const unsigned m = __ballot_sync(full, acc);
+                    const int ru = r + __popc(m & lt);
+                    if (acc && ru < cap) S.list[i][ru] = sj[u];
+                    r += __popc(m);
+                }
+                if (lane == i) cnt = r;
+            }
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kWcWarps * 32, 4)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
@@ -178,11 +301,11 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         }
         if (home) S.home[lane] = pi;
         // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
+        const int D0 = sc.dims[0], D1 = sc.dims[1];
+        const int vx = local % D0, vy = (local / D0) % D1, vz = local / (D0 * D1);
         int ck = 0, stk = 0;
         if (lane < 27) {
-            const int D0 = sc.dims[0], D1 = sc.dims[1];
             const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
-            const int vx = local % D0, vy = (local / D0) % D1, vz = local / (D0 * D1);
             const int nx = vx + lane / 9 - 1, ny = vy + (lane / 3) % 3 - 1, nz = vz + lane % 3 - 1;
             if (nx >= 0 && nx < w0 && ny >= 0 && ny < w1 && nz >= 0 && nz < w2) {
                 const int id = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
@@ -208,81 +331,17 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         __syncwarp();
         const float h2_lo = sc.h2_lo, h2_hi = sc.h2_hi;
         const double h_d = sc.h_d;
-        const float inf = __int_as_float(0x7f800000);
-        const unsigned le = (2u << lane) - 1u;      // bits 0..lane
+        // Dense neighbourhoods: each home particle's 27-bit mask of the walk
+        // voxels within h of it (box distance, the walk's culling test), so
+        // that a batch lying in voxels it cannot reach is skipped for it.
+        // Those voxels hold no accepted candidate: the result is unchanged.
+        const bool cull = !sc.walk_trunc && M > kWcCullMin;
         int cnt = 0;    // lane i: accepted candidates of home particle i so far
-        for (int b0 = 0; b0 < M; b0 += kWcBatch) {
-            // home particles still below the cap
-            const unsigned todo = __ballot_sync(full, home && cnt < cap);
-            if (!todo) break;
-            // Batch candidates q = b0 + 32 u + lane.  Bw[u] bit l: a non-empty
-            // walk voxel starts at q = b0 + 32 u + l (l >= 1 when u = 0); the
-            // rank of the voxel holding q is the number of non-empty voxels
-            // starting at or before b0, minus one, plus the set bits up to q.
-            const int pk = Pk - b0;
-            unsigned Bw[kWcPerLane];
-#pragma unroll
-            for (int u = 0; u < kWcPerLane; ++u)
-                Bw[u] = __reduce_or_sync(
-                    full, (nzk && pk >= 1 && (pk >> 5) == u) ? (1u << (pk & 31)) : 0u);
-            int rank = __popc(__ballot_sync(full, nzk && pk <= 0)) - 1;
-            // past the end of the walk: +inf coordinates, never within h
-            float4 pj[kWcPerLane];
-            int sj[kWcPerLane];
-#pragma unroll
-            for (int u = 0; u < kWcPerLane; ++u) {
-                const int q = b0 + 32 * u + lane;
-                pj[u] = make_float4(inf, inf, inf, 0.f);
-                sj[u] = -1;
-                if (q < M) {
-                    sj[u] = q + S.off[rank + __popc(Bw[u] & le)];
-                    pj[u] = __ldg(pos + sj[u]);
-                }
-                rank += __popc(Bw[u]);
-            }
-            // Fast pass: FP32 decisions only.  A pair in the FP32 guard band
-            // around h^2 is rare; if any occurs, the whole batch is redone from
-            // the counts it started with, deciding those pairs in FP64.  Every
-            // list entry below the final counts is rewritten by the redo.
-            const int cnt0 = cnt;
-            bool band_seen = false;
-            for (unsigned t = todo; t; t &= t - 1) {
-                const int i = __ffs(t) - 1;
-                int r = __shfl_sync(full, cnt, i);
-                const float4 ph = S.home[i];
-#pragma unroll
-                for (int u = 0; u < kWcPerLane; ++u) {
-                    const float d2 = dist2(ph, pj[u]);
-                    const bool acc = d2 < h2_lo;
-                    band_seen |= !acc && d2 <= h2_hi;
-                    const unsigned m = __ballot_sync(full, acc);
-                    const int ru = r + __popc(m & lt);
-                    if (acc && ru < cap) S.list[i][ru] = sj[u];
-                    r += __popc(m);
-                }
-                if (lane == i) cnt = r;
-            }
-            if (__any_sync(full, band_seen)) {
-                cnt = cnt0;
-                for (unsigned t = todo; t; t &= t - 1) {
-                    const int i = __ffs(t) - 1;
-                    int r = __shfl_sync(full, cnt, i);
-                    const float4 ph = S.home[i];
-#pragma unroll
-                    for (int u = 0; u < kWcPerLane; ++u) {
-                        const float d2 = dist2(ph, pj[u]);
-                        bool acc = d2 < h2_lo;
-                        if (!acc && d2 <= h2_hi)
-                            acc = within_exact(ph.x, ph.y, ph.z, pj[u].x, pj[u].y, pj[u].z, h_d);
-                        const unsigned m = __ballot_sync(full, acc);
-                        const int ru = r + __popc(m & lt);
-                        if (acc && ru < cap) S.list[i][ru] = sj[u];
-                        r += __popc(m);
-                    }
-                    if (lane == i) cnt = r;
-                }
-            }
-        }
+        if (cull)
+            wc_candidates<true>(S, cnt, home, cap, M, Pk, ck, nzk, reach_mask(pi, vx, vy, vz, sc),
+                                pos, h2_lo, h2_hi, h_d);
+        else
+            wc_candidates<false>(S, cnt, home, cap, M, Pk, ck, nzk, 0u, pos, h2_lo, h2_hi, h_d);
         __syncwarp();
         // (a) one lane per list entry: the density term of every accepted pair
         // replaces the entry (self gets kSelfTerm), and each particle's list
