@@ -934,13 +934,15 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     double* sr = ctx->stage + 6 * N;
     const size_t b3 = sizeof(double) * 3 * N;
     const int nb = blocks(ctx->n);
-    // Two streams.  st: position upload, the step, position and velocity
-    // download.  st2: the velocity upload, queued behind the position upload
-    // (they share the host link) so that the voxel sort and the density pass,
-    // which need positions only, run while it is in flight (the step gathers
-    // the velocities into slot order after the density pass); then, once the
-    // density pass is done, the density download, which overlaps the force
-    // pass.  Results are the same bits as the one-stream sequence.
+    // Two streams.  st: position upload and the step.  st2: the velocity
+    // upload, queued behind the position upload (they share the host link) so
+    // that the voxel sort and the density pass, which need positions only, run
+    // while it is in flight (the step gathers the velocities into slot order
+    // after the density pass); then, once the density pass is done, the
+    // density download, which overlaps the force pass.  The next positions and
+    // velocities are downloaded whole from st after the force pass (slot
+    // order), or range by range from st2 while st computes the next range
+    // (particle order).  Results are the same bits as the one-stream sequence.
     SPHGB_CUDA(cudaEventRecord(e_start, st));
     SPHGB_CUDA(cudaStreamWaitEvent(st2, e_start, 0));
     SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, b3, cudaMemcpyHostToDevice, st));
