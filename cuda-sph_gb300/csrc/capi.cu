@@ -57,6 +57,7 @@ struct ConsChunk {
 // host-buffer entry point: particle-order ranges of the force pass, and its events
 // (start, positions in, velocities in, density done, slot map ready, downloads
 // queued, then one per range)
+constexpr int64_t kMaxParticles = SPHGB_MAX_PARTICLES;
 constexpr int kHostRanges = 8;
 constexpr int kHostFirstRangeEvent = 6;
 constexpr int kHostEvents = kHostFirstRangeEvent + kHostRanges;
@@ -579,8 +580,11 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
         hp[i] = (int32_t)n_tot;
         n_tot += scenes[i].particle_count;
         v_tot += d.v_count + 1;   // + the scene's overflow bucket
-        if (n_tot > (int64_t)0x7fffffff - 1 || v_tot > (int64_t)0x7fffffff - 1)
-            return fail(SPHGB_ERR_RANGE, "particles or voxels over 2^31 in one context");
+        // kernels index per-particle rows (3 doubles, 2 float4) in 32-bit arithmetic
+        if (n_tot > kMaxParticles)
+            return fail(SPHGB_ERR_RANGE, "more than 2^29 particles in one context");
+        if (v_tot > (int64_t)0x7fffffff - 1)
+            return fail(SPHGB_ERR_RANGE, "voxel tables over 2^31 entries in one context");
         if (d.mode == SPHGB_MODE_PIPE) any_pipe = true;
     }
     hp[n_scenes] = (int32_t)n_tot;

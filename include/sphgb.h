@@ -96,7 +96,9 @@ const char* sphgb_last_error(void);
  * abstract_sph_strategy.py:18-29); with many it is the batched path.
  * pipe_rows_table: host doubles [total rows][5] in Pipe.to_numpy() layout
  * (common/data_classes.py:34-44); may be NULL when no scene is in pipe mode.
- * Allocates all scratch with cudaMalloc on the current device. */
+ * Allocates all scratch with cudaMalloc on the current device.  At most
+ * SPHGB_MAX_PARTICLES particles over all scenes (SPHGB_ERR_RANGE beyond). */
+#define SPHGB_MAX_PARTICLES (1 << 29)
 int sphgb_ctx_create(const SphgbSceneParams* scenes, int n_scenes,
                      const double* pipe_rows_table, int n_pipe_rows_total,
                      SphgbCtx** out_ctx);
