@@ -1,10 +1,9 @@
 """Autotuner for the launch choices of a batch of scenes.
 
 Tunes what changes speed but not results:
-* the density kernel variant: one warp per voxel run (SPHGB_DENSITY_WARP),
-  best when voxels hold few particles, or one thread per particle with
-  per-particle voxel culling and early exit (SPHGB_DENSITY_THREAD), best in
-  dense scenes;
+* the density kernel variant: one warp per voxel run, a lane per candidate
+  (SPHGB_DENSITY_WARP), or one thread per particle with its own walk
+  (SPHGB_DENSITY_THREAD); both skip voxels beyond h and stop at the cap;
 * the block size of the per-particle sort kernels;
 * the member count above which a voxel is sorted by a block of its own.
 
