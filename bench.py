@@ -79,8 +79,11 @@ def parse_args():
     ap.add_argument("--tuning", choices=["auto", "default", "warp", "thread"],
                     default="auto", help="launch tuning: autotuned on the scene, the library "
                     "defaults, or the defaults with the named density kernel")
-    ap.add_argument("--served-requests", type=int, default=24)
-    ap.add_argument("--served-rate", type=float, default=64.0, help="Poisson arrivals per second")
+    ap.add_argument("--served-requests", type=int, default=48)
+    ap.add_argument("--served-rate", type=float, default=64.0,
+                    help="Poisson arrivals per second of the headline served entry")
+    ap.add_argument("--served-rates", default="16,64,256",
+                    help="comma-separated arrival rates of the served sweep")
     return ap.parse_args()
 
 
@@ -449,20 +452,17 @@ def pipe_section(args):
 def served_section(args):
     """Served workload: Poisson arrivals, 70 % box / 30 % pipe, N log-uniform
     in [2048, 524288], steps uniform in [100, 2000], 150 GB HBM budget;
-    continuous batching against serving the same requests one at a time."""
-    import numpy as np
+    continuous batching against serving the same requests one at a time.
+    The arrival rate is swept: the same requests (sizes, steps, start states)
+    arrive at each rate, their arrival times scaled."""
+    import dataclasses
     from sphgb.device import SceneBatch
     from sphgb.serve import SceneServer, poisson_requests
-    reqs = poisson_requests(args.served_rate, args.served_requests, seed=4)
-    work = sum(r.spec.n * r.steps for r in reqs)
-    server = SceneServer(hbm_budget_bytes=150e9, max_tick_steps=64)
-    st = server.run(reqs)
-    server.close()
-    log(f"served: {st.requests} requests, {work} particle-steps in {st.wall_s:.3f} s, "
-        f"p50 {st.pct(50):.3f} s p99 {st.pct(99):.3f} s, max active {st.max_active}")
     import torch
+    base = poisson_requests(1.0, args.served_requests, seed=4)     # arrivals at rate 1
+    work = sum(r.spec.n * r.steps for r in base)
     plain_s = 0.0
-    for r in reqs:
+    for r in base:
         b = SceneBatch([r.spec])
         b.load_states([r.state])
         torch.cuda.synchronize()
@@ -473,12 +473,23 @@ def served_section(args):
         torch.cuda.synchronize()
         plain_s += e0.elapsed_time(e1) / 1e3
         b.close()
-    log(f"served one at a time: {plain_s:.3f} s of GPU time")
-    return {"requests": st.requests, "rate_per_s": args.served_rate, "value": st.throughput,
-            "unit": "particle-steps/s", "wall_s": st.wall_s, "p50_latency_s": st.pct(50),
-            "p99_latency_s": st.pct(99), "max_active": st.max_active, "ticks": st.ticks,
-            "repacks": st.repacks, "plain_value": work / plain_s,
-            "vs_plain": (work / st.wall_s) / (work / plain_s), "hbm_budget_gb": 150}
+    log(f"served one at a time: {plain_s:.3f} s of GPU time for {work} particle-steps")
+    rates = sorted({float(x) for x in args.served_rates.split(",")} | {args.served_rate})
+    sweep = []
+    for rate in rates:
+        reqs = [dataclasses.replace(r, arrival=r.arrival / rate) for r in base]
+        server = SceneServer(hbm_budget_bytes=150e9, max_tick_steps=64)
+        st = server.run(reqs)
+        server.close()
+        log(f"served at {rate:g}/s: {st.requests} requests in {st.wall_s:.3f} s, "
+            f"p50 {st.pct(50):.3f} s p99 {st.pct(99):.3f} s, max active {st.max_active}")
+        sweep.append({"rate_per_s": rate, "value": st.throughput, "wall_s": st.wall_s,
+                      "p50_latency_s": st.pct(50), "p99_latency_s": st.pct(99),
+                      "max_active": st.max_active, "ticks": st.ticks, "repacks": st.repacks,
+                      "vs_plain": st.throughput / (work / plain_s)})
+    head = next(s for s in sweep if s["rate_per_s"] == args.served_rate)
+    return {"requests": len(base), "particle_steps": work, "unit": "particle-steps/s",
+            "plain_value": work / plain_s, "hbm_budget_gb": 150, **head, "sweep": sweep}
 
 
 def run_reference(args):
