@@ -8,6 +8,7 @@
 // which is VoxelSPHStrategy.compute_next_state (sim/src/sph/strategies/
 // abstract_sph_strategy.py:31-46, voxel_sph_strategy.py:20-116) without any
 // host round trip.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -66,12 +67,17 @@ struct SphgbCtx {
     int device = 0;
     int n_scenes = 0;
     int n = 0;
-    int v_total = 0;
-    int n_tiles = 0;
+    // Two voxel-table layouts of the same scenes: the fused step's (4x4x4
+    // tiles) and the reference's row-major one, which every stage entry point
+    // and sphgb_ctx_sizes use.
+    int v_total = 0;           // step layout
+    int v_total_ref = 0;       // reference layout
+    int layout = 0;            // step layout: 0 all row-major, 1 all tiled, 2 mixed
     bool any_pipe = false;
     std::vector<SceneDev> h_scenes;
     std::vector<int32_t> h_pbegin;
-    SceneDev* d_scenes = nullptr;
+    SceneDev* d_scenes = nullptr;       // step layout
+    SceneDev* d_scenes_ref = nullptr;   // reference layout
     int32_t* d_pbegin = nullptr;
     double* d_pipe = nullptr;
     int n_pipe_rows = 0;
@@ -115,7 +121,7 @@ struct SphgbCtx {
     double* d_partials = nullptr;
     // buffer capacities (elements), so reconfiguration reuses what is big enough
     struct {
-        size_t scenes = 0, pbegin = 0, pipe = 0, cell = 0, slot_of = 0, slot = 0, tmp_pid = 0,
+        size_t scenes = 0, scenes_ref = 0, pbegin = 0, pipe = 0, cell = 0, slot_of = 0, slot = 0, tmp_pid = 0,
                vstart = 0,
                vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, fin = 0, big_list = 0,
                big_count = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
@@ -138,13 +144,14 @@ struct SphgbCtx {
     double host_ms[3] = {};     // timed call per order (index = order)
     std::map<int, cudaGraphExec_t> graphs;
 
-    Launch launch(cudaStream_t st) const {
+    Launch launch(cudaStream_t st, bool ref_layout = false) const {
         Launch L;
-        L.scenes = d_scenes;
+        L.scenes = ref_layout ? d_scenes_ref : d_scenes;
         L.pbegin = d_pbegin;
         L.n_scenes = n_scenes;
         L.n = n;
-        L.v_total = v_total;
+        L.v_total = ref_layout ? v_total_ref : v_total;
+        L.layout = ref_layout ? 0 : layout;
         L.pipe = d_pipe;
         L.pipe_scenes = any_pipe;
         L.sort_block = sort_block;
@@ -171,7 +178,7 @@ int dalloc(T** p, size_t count) {
 void free_ctx(SphgbCtx* c) {
     if (!c) return;
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
-    void* ptrs[] = {c->d_scenes, c->d_pbegin, c->d_pipe, c->cell, c->slot_of, c->slot, c->tmp_pid,
+    void* ptrs[] = {c->d_scenes, c->d_scenes_ref, c->d_pbegin, c->d_pipe, c->cell, c->slot_of, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->fin, c->owned, c->stage, c->d_chunks, c->d_partials,
                     c->big_list, c->big_count, c->nbr.idx, c->nbr.count, c->tasks};
@@ -197,7 +204,8 @@ float round_up_f(double x) {
     return f;
 }
 
-int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d) {
+int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d,
+                bool tiled = false) {
     std::memset(&d, 0, sizeof(d));
     if (p.particle_count < 0) return fail(SPHGB_ERR_INVALID, "particle_count < 0");
     if (!(p.inf_r > 0.0) || !std::isfinite(p.inf_r)) return fail(SPHGB_ERR_INVALID, "inf_r must be > 0");
@@ -224,8 +232,17 @@ int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d) {
         nv *= d.dims[a];
         if (nv > (int64_t)0x7fffffff) return fail(SPHGB_ERR_RANGE, "voxel table over 2^31 entries");
     }
-    d.v_count = (int32_t)nv;
     d.walk_trunc = (d.wdims[0] != d.dims[0] || d.wdims[1] != d.dims[1] || d.wdims[2] != d.dims[2]);
+    if (tiled && !d.walk_trunc) {
+        // 4x4x4 tiles (voxel_index); a truncated walk keeps the reference's
+        // row-major ids, which it addresses with its own strides
+        d.tiled = 1;
+        d.nt0 = (d.dims[0] + 3) / 4;
+        d.nt1 = (d.dims[1] + 3) / 4;
+        nv = (int64_t)d.nt0 * d.nt1 * ((d.dims[2] + 3) / 4) * 64;
+        if (nv > (int64_t)0x7fffffff) return fail(SPHGB_ERR_RANGE, "voxel table over 2^31 entries");
+    }
+    d.v_count = (int32_t)nv;
     const float h = (float)p.inf_r;
     const double hd = (double)h;
     d.h = h;
@@ -465,11 +482,11 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                      int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
                      cudaEvent_t* ev = nullptr, bool with_tasks = false) {
     cudaStream_t st = L.stream;
-    if (c->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * c->v_total, st));
+    if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * L.v_total, st));
     SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 2 * sizeof(int32_t), st));
     SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
-    SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, c->n_tiles));
+    SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, scan_tiles(L.v_total)));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[1], st));
     SPHGB_CUDA(launch_scatter(L, c->cell, c->slot, pid, vstart, vcount, c->tmp_pid, c->big_list,
                               c->big_count));
@@ -566,24 +583,27 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     if (!scenes || n_scenes <= 0) return fail(SPHGB_ERR_INVALID, "need at least one scene");
     if (n_pipe_rows_total < 0 || (n_pipe_rows_total > 0 && !pipe_rows_table))
         return fail(SPHGB_ERR_INVALID, "bad pipe table");
-    std::vector<SceneDev> hs((size_t)n_scenes);
+    std::vector<SceneDev> hs((size_t)n_scenes), hr((size_t)n_scenes);
     std::vector<int32_t> hp((size_t)n_scenes + 1);
-    int64_t n_tot = 0, v_tot = 0;
+    int64_t n_tot = 0, v_tot = 0, v_tot_ref = 0;
     bool any_pipe = false;
     for (int i = 0; i < n_scenes; ++i) {
-        int rc = build_scene(scenes[i], n_pipe_rows_total, hs[i]);
+        int rc = build_scene(scenes[i], n_pipe_rows_total, hs[i], true);
+        if (!rc) rc = build_scene(scenes[i], n_pipe_rows_total, hr[i], false);
         if (rc) return fail(rc, "scene " + std::to_string(i) + ": " + g_last_error);
         SceneDev& d = hs[i];
-        d.p_begin = (int32_t)n_tot;
-        d.p_count = (int32_t)scenes[i].particle_count;
+        d.p_begin = hr[i].p_begin = (int32_t)n_tot;
+        d.p_count = hr[i].p_count = (int32_t)scenes[i].particle_count;
         d.v_begin = (int32_t)v_tot;
+        hr[i].v_begin = (int32_t)v_tot_ref;
         hp[i] = (int32_t)n_tot;
         n_tot += scenes[i].particle_count;
         v_tot += d.v_count + 1;   // + the scene's overflow bucket
+        v_tot_ref += hr[i].v_count + 1;
         // kernels index per-particle rows (3 doubles, 2 float4) in 32-bit arithmetic
         if (n_tot > kMaxParticles)
             return fail(SPHGB_ERR_RANGE, "more than 2^29 particles in one context");
-        if (v_tot > (int64_t)0x7fffffff - 1)
+        if (v_tot > (int64_t)0x7fffffff - 1 || v_tot_ref > (int64_t)0x7fffffff - 1)
             return fail(SPHGB_ERR_RANGE, "voxel tables over 2^31 entries in one context");
         if (d.mode == SPHGB_MODE_PIPE) any_pipe = true;
     }
@@ -594,11 +614,12 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
         for (int b = 0; b < d.p_count; b += kConsChunk)
             chunks.push_back({i, d.p_begin + b, d.p_begin + std::min(d.p_count, b + kConsChunk), 0});
     }
-    const size_t N = (size_t)n_tot, V = (size_t)v_tot;
-    const int n_tiles = scan_tiles((int)v_tot);
+    const size_t N = (size_t)n_tot, V = (size_t)std::max(v_tot, v_tot_ref);
+    const int n_tiles = scan_tiles((int)V);
     auto& k = c->cap;
     int rc = SPHGB_OK;
     rc = rc ? rc : ensure(&c->d_scenes, k.scenes, (size_t)n_scenes);
+    rc = rc ? rc : ensure(&c->d_scenes_ref, k.scenes_ref, (size_t)n_scenes);
     rc = rc ? rc : ensure(&c->d_pbegin, k.pbegin, (size_t)n_scenes + 1);
     rc = rc ? rc : ensure(&c->d_pipe, k.pipe, (size_t)n_pipe_rows_total * 5);
     rc = rc ? rc : ensure(&c->cell, k.cell, N);
@@ -623,6 +644,8 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     if (rc) return rc;
     SPHGB_CUDA(cudaMemcpy(c->d_scenes, hs.data(), sizeof(SceneDev) * n_scenes,
                           cudaMemcpyHostToDevice));
+    SPHGB_CUDA(cudaMemcpy(c->d_scenes_ref, hr.data(), sizeof(SceneDev) * n_scenes,
+                          cudaMemcpyHostToDevice));
     SPHGB_CUDA(cudaMemcpy(c->d_pbegin, hp.data(), sizeof(int32_t) * (n_scenes + 1),
                           cudaMemcpyHostToDevice));
     if (n_pipe_rows_total > 0)
@@ -636,7 +659,10 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     c->n_scenes = n_scenes;
     c->n = (int)n_tot;
     c->v_total = (int)v_tot;
-    c->n_tiles = n_tiles;
+    c->v_total_ref = (int)v_tot_ref;
+    int n_tiled = 0;
+    for (const SceneDev& d : c->h_scenes) n_tiled += d.tiled;
+    c->layout = n_tiled == 0 ? 0 : (n_tiled == n_scenes ? 1 : 2);
     c->n_pipe_rows = n_pipe_rows_total;
     c->n_chunks = (int)chunks.size();
     c->any_pipe = any_pipe;
@@ -741,7 +767,7 @@ int sphgb_ctx_destroy(SphgbCtx* ctx) {
 int sphgb_ctx_sizes(const SphgbCtx* ctx, int64_t* n_particles, int64_t* n_voxels) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (n_particles) *n_particles = ctx->n;
-    if (n_voxels) *n_voxels = ctx->v_total;
+    if (n_voxels) *n_voxels = ctx->v_total_ref;
     return SPHGB_OK;
 }
 
@@ -1073,8 +1099,8 @@ int sphgb_assign_voxels(SphgbCtx* ctx, const float* d_pos, int32_t* d_voxel_out,
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (ctx->n > 0 && (!d_pos || !d_voxel_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
-    const Launch L = ctx->launch(st);
-    if (ctx->v_total > 0) SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * ctx->v_total, st));
+    const Launch L = ctx->launch(st, true);
+    if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * L.v_total, st));
     SPHGB_CUDA(launch_hash_count(L, reinterpret_cast<const float4*>(d_pos), d_voxel_out, ctx->slot,
                                  ctx->vcount));
     return SPHGB_OK;
@@ -1091,7 +1117,7 @@ int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
     if ((d_pos64 == nullptr) != (d_pos64_out == nullptr))
         return fail(SPHGB_ERR_INVALID, "pass both FP64 position buffers or neither");
     cudaStream_t st = as_stream(stream);
-    const Launch L = ctx->launch(st);
+    const Launch L = ctx->launch(st, true);
     return enqueue_organize(ctx, L, reinterpret_cast<const float4*>(d_pos),
                             reinterpret_cast<const float4*>(d_vel), d_pid, d_pos64,
                             reinterpret_cast<float4*>(d_pos_out),
@@ -1105,7 +1131,7 @@ int sphgb_neighbours(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (d_list && list_stride <= 0) return fail(SPHGB_ERR_INVALID, "list_stride must be > 0");
     cudaStream_t st = as_stream(stream);
-    SPHGB_CUDA(launch_neighbours(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
+    SPHGB_CUDA(launch_neighbours(ctx->launch(st, true), reinterpret_cast<const float4*>(d_pos_sorted),
                                  d_voxel_start, d_voxel_count, d_list, list_stride, d_count_capped,
                                  d_count_uncapped));
     return SPHGB_OK;
@@ -1116,7 +1142,7 @@ int sphgb_density(SphgbCtx* ctx, const float* d_pos_sorted, const int32_t* d_vox
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (ctx->n > 0 && (!d_pos_sorted || !d_rho_out)) return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
-    SPHGB_CUDA(launch_density(ctx->launch(st), reinterpret_cast<const float4*>(d_pos_sorted),
+    SPHGB_CUDA(launch_density(ctx->launch(st, true), reinterpret_cast<const float4*>(d_pos_sorted),
                               nullptr, d_voxel_start, d_voxel_count, d_rho_out, nullptr,
                               NbrList{}));
     return SPHGB_OK;
@@ -1131,7 +1157,7 @@ int sphgb_forces(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel_so
                        !d_viscosity_out))
         return fail(SPHGB_ERR_INVALID, "null buffer");
     cudaStream_t st = as_stream(stream);
-    const Launch L = ctx->launch(st);
+    const Launch L = ctx->launch(st, true);
     SPHGB_CUDA(launch_force_inputs(L, reinterpret_cast<const float4*>(d_pos_sorted),
                                    reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
                                    ctx->fin));
@@ -1155,7 +1181,7 @@ int sphgb_integrate(SphgbCtx* ctx, const float* d_pos_sorted, const float* d_vel
     if (ctx->any_pipe && ctx->n > 0 && (!d_pos64_sorted || !d_pos64_out))
         return fail(SPHGB_ERR_INVALID, "pipe scenes need the FP64 position buffers");
     cudaStream_t st = as_stream(stream);
-    const Launch L = ctx->launch(st);
+    const Launch L = ctx->launch(st, true);
     SPHGB_CUDA(launch_force_inputs(L, reinterpret_cast<const float4*>(d_pos_sorted),
                                    reinterpret_cast<const float4*>(d_vel_sorted), d_rho_sorted,
                                    ctx->fin));

@@ -71,7 +71,7 @@ k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
         const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
         const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
-        vid = sc.v_begin + vx + vy * sc.dims[0] + vz * sc.dims[0] * sc.dims[1];
+        vid = sc.v_begin + voxel_index(vx, vy, vz, sc.tiled, sc.dims[0], sc.dims[1], sc.nt0, sc.nt1);
     } else {
         vid = sc.v_begin + sc.v_count;   // overflow bucket
     }

@@ -47,9 +47,25 @@ struct SceneDev {
     int32_t mode;               // 0 box, 1 pipe
     int32_t walk_trunc;         // 1 when wdims != dims (no voxel culling then)
     int32_t pipe_off, pipe_rows;
+    int32_t tiled;              // 1: voxel table in 4x4x4 tiles (see voxel_index), 0: row-major
+    int32_t nt0, nt1;           // tiles along x and y when tiled
     int32_t pad;
     uint64_t seed;
 };
+
+// Table index of voxel (x, y, z) of a scene.  Row-major, x fastest (the
+// reference's compute_1d_idx, voxel_kernels.py:14-17, with the stride dims
+// d0, d1), or, for the fused step, in 4x4x4 tiles: tile (x/4, y/4, z/4) in
+// row-major tile order, 64 voxels per tile, x fastest inside.  Tiles keep
+// spatial neighbours close in the sorted state, which the passes that gather
+// neighbour data read through L1.
+__host__ __device__ __forceinline__ int voxel_index(int x, int y, int z, int tiled, int d0, int d1,
+                                                    int nt0, int nt1) {
+    if (tiled)
+        return ((((z >> 2) * nt1 + (y >> 2)) * nt0 + (x >> 2)) << 6) | ((z & 3) << 4) |
+               ((y & 3) << 2) | (x & 3);
+    return x + y * d0 + z * d0 * d1;
+}
 
 // ---- scene lookup ---------------------------------------------------------
 // pbegin has n_scenes + 1 entries (prefix of particle counts).
@@ -125,6 +141,7 @@ struct WalkGeom {
     double h_d;
     int cap;
     bool cull;
+    int tiled, nt0, nt1;
 };
 
 __device__ __forceinline__ WalkGeom load_geom(const SceneDev& sc) {
@@ -137,6 +154,9 @@ __device__ __forceinline__ WalkGeom load_geom(const SceneDev& sc) {
     g.h_d = sc.h_d;
     g.cap = sc.cap;
     g.cull = !sc.walk_trunc;
+    g.tiled = sc.tiled;
+    g.nt0 = sc.nt0;
+    g.nt1 = sc.nt1;
     return g;
 }
 
@@ -146,7 +166,9 @@ __device__ __forceinline__ WalkGeom load_geom(const SceneDev& sc) {
 // (self included, :77-84).  visit(j, dx, dy, dz, d2) is called per accepted
 // neighbour slot j.  Returns the number accepted.  A particle with a
 // non-finite coordinate has no neighbours (every distance test fails).
-template <class Visit>
+// kLayout: the scene's voxel table is row-major (0), tiled (1), or either,
+// read from g.tiled (2).
+template <int kLayout = 2, class Visit>
 __device__ __forceinline__ int walk(const float4 pi, const WalkGeom& g,
                                     const int32_t* __restrict__ vstart,
                                     const int32_t* __restrict__ vcount,
@@ -179,7 +201,8 @@ __device__ __forceinline__ int walk(const float4 pi, const WalkGeom& g,
                 const int nz = cz + ddz - 1;
                 if (nz < 0 || nz >= g.w2) continue;
                 if (g.cull && gxy + (ddz == 0 ? gz0 : (ddz == 2 ? gz2 : 0.0f)) > g.cull2) continue;
-                const int vid = g.v_begin + nx + ny * g.w0 + nz * g.w0 * g.w1;
+                const int tiled = kLayout == 2 ? g.tiled : kLayout;
+                const int vid = g.v_begin + voxel_index(nx, ny, nz, tiled, g.w0, g.w1, g.nt0, g.nt1);
                 const int c = __ldg(vcount + vid);
                 if (c == 0) continue;
                 const int s0 = __ldg(vstart + vid);
@@ -384,6 +407,7 @@ struct Launch {
     bool pipe_scenes;           // some scene is in pipe mode
     int sort_block = kBlock;    // threads per block of the per-particle sort kernels
     int big_voxel = 64;         // voxels above this many members are sorted per block
+    int layout = 0;             // voxel tables: 0 all row-major, 1 all tiled, 2 mixed
     cudaStream_t stream;
 };
 

@@ -43,7 +43,8 @@ __device__ __forceinline__ void write_force_inputs(int s, const float4& pi, cons
 // One particle's density by a thread-private walk: the walk records neighbour
 // slots in row[k * stride] (k < kListCap), the sum runs afterwards in walk
 // order; with more neighbours than that the walk is repeated, summing.
-// fin (with vel) is optional.
+// fin (with vel) is optional.  kLayout: see walk().
+template <int kLayout>
 __device__ __forceinline__ void density_one(int s, const float4& pi, const SceneDev& sc,
                                             const float4* __restrict__ pos,
                                             const float4* __restrict__ vel,
@@ -53,7 +54,7 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
                                             const NbrList& nbr, int32_t* row, int stride) {
     const WalkGeom g = load_geom(sc);
     int others = 0;
-    walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
+    walk<kLayout>(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
         if (j != s) {
             if (others < kListCap) row[others * stride] = j;
             ++others;
@@ -79,7 +80,7 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
     } else {
         // more neighbours than the list holds (no cap or a cap above it):
         // walk again, summing on the way
-        walk(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
+        walk<kLayout>(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float d2) {
             if (j != s) {
                 const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
                 acc.add(u * u * u);
@@ -94,6 +95,7 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
 
 // thread per particle (used by the stage entry points and as the reference
 // path of the warp-cooperative kernel below)
+template <int kLayout>
 __global__ void __launch_bounds__(kBlock)
 k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
           int n, const float4* __restrict__ pos, const float4* __restrict__ vel,
@@ -103,8 +105,8 @@ k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegi
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
-    density_one(s, __ldg(pos + s), sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
-                &s_list[0][threadIdx.x], kBlock);
+    density_one<kLayout>(s, __ldg(pos + s), sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
+                         &s_list[0][threadIdx.x], kBlock);
 }
 
 // squared distance with the walk's arithmetic (within() in sphgb_internal.cuh)
@@ -267,6 +269,8 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
     }
 }
 
+// kLayout: 0 every scene's voxel table row-major, 1 every one tiled, 2 per scene
+template <int kLayout>
 __global__ void __launch_bounds__(kWcWarps * 32, 4)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
              int n_scenes, int n, const float4* __restrict__ pos,
@@ -295,20 +299,33 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home) density_one(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr, &S.list[lane][0], 1);
+            if (home)
+                density_one<kLayout>(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
+                                     &S.list[lane][0], 1);
             __syncwarp();
             continue;
         }
         if (home) S.home[lane] = pi;
         // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
-        const int D0 = sc.dims[0], D1 = sc.dims[1];
-        const int vx = local % D0, vy = (local / D0) % D1, vz = local / (D0 * D1);
+        const int tiled = kLayout == 2 ? sc.tiled : kLayout;
+        int vx, vy, vz;
+        if (tiled) {
+            const int tl = local >> 6, in = local & 63;
+            vx = ((tl % sc.nt0) << 2) | (in & 3);
+            vy = (((tl / sc.nt0) % sc.nt1) << 2) | ((in >> 2) & 3);
+            vz = ((tl / (sc.nt0 * sc.nt1)) << 2) | (in >> 4);
+        } else {
+            const int D0 = sc.dims[0], D1 = sc.dims[1];
+            vx = local % D0;
+            vy = (local / D0) % D1;
+            vz = local / (D0 * D1);
+        }
         int ck = 0, stk = 0;
         if (lane < 27) {
             const int w0 = sc.wdims[0], w1 = sc.wdims[1], w2 = sc.wdims[2];
             const int nx = vx + lane / 9 - 1, ny = vy + (lane / 3) % 3 - 1, nz = vz + lane % 3 - 1;
             if (nx >= 0 && nx < w0 && ny >= 0 && ny < w1 && nz >= 0 && nz < w2) {
-                const int id = sc.v_begin + nx + ny * w0 + nz * w0 * w1;
+                const int id = sc.v_begin + voxel_index(nx, ny, nz, tiled, w0, w1, sc.nt0, sc.nt1);
                 ck = __ldg(vcount + id);
                 stk = __ldg(vstart + id);
             }
@@ -697,8 +714,9 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel
                            const int32_t* vstart, const int32_t* vcount, float* rho,
                            float4* fin, NbrList nbr) {
     if (L.n == 0) return cudaSuccess;
-    k_density<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                         vel, vstart, vcount, rho, fin, nbr);
+    auto kernel = L.layout == 1 ? k_density<1> : L.layout == 2 ? k_density<2> : k_density<0>;
+    kernel<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
+                                                     vstart, vcount, rho, fin, nbr);
     return cudaGetLastError();
 }
 
@@ -710,9 +728,9 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
     // persistent grid: up to 4 blocks of 8 warps per SM, warps stride over the tasks
     int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
     if (blocks > 152 * 4) blocks = 152 * 4;
-    k_density_wc<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                         vel, vstart, vcount, rho, fin, nbr, tasks,
-                                                         task_count);
+    auto kernel = L.layout == 1 ? k_density_wc<1> : L.layout == 2 ? k_density_wc<2> : k_density_wc<0>;
+    kernel<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
+                                                   vstart, vcount, rho, fin, nbr, tasks, task_count);
     return cudaGetLastError();
 }
 
