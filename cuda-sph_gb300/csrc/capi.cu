@@ -59,6 +59,7 @@ struct ConsChunk {
 // (start, positions in, velocities in, density done, slot map ready, downloads
 // queued, then one per range)
 constexpr int64_t kMaxParticles = SPHGB_MAX_PARTICLES;
+constexpr double kTileMaxOccupancy = 8.0;   // particles per voxel, table mean
 constexpr int kHostRanges = 8;
 constexpr int kHostFirstRangeEvent = 6;
 constexpr int kHostEvents = kHostFirstRangeEvent + kHostRanges;
@@ -233,9 +234,13 @@ int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d,
         if (nv > (int64_t)0x7fffffff) return fail(SPHGB_ERR_RANGE, "voxel table over 2^31 entries");
     }
     d.walk_trunc = (d.wdims[0] != d.dims[0] || d.wdims[1] != d.dims[1] || d.wdims[2] != d.dims[2]);
-    if (tiled && !d.walk_trunc) {
-        // 4x4x4 tiles (voxel_index); a truncated walk keeps the reference's
-        // row-major ids, which it addresses with its own strides
+    if (tiled && !d.walk_trunc && (double)p.particle_count <= kTileMaxOccupancy * (double)nv) {
+        // 4x4x4 tiles (voxel_index) for sparse scenes, where they shorten the
+        // gathers of the force pass.  Dense scenes stay row-major: their
+        // voxels fill L1 anyway, and the histogram counters of a cluster
+        // would share cache lines, serialising the hash's atomics.  A
+        // truncated walk keeps the reference's row-major ids, which it
+        // addresses with its own strides.
         d.tiled = 1;
         d.nt0 = (d.dims[0] + 3) / 4;
         d.nt1 = (d.dims[1] + 3) / 4;

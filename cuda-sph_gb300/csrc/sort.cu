@@ -4,7 +4,8 @@
 // (sim/src/sph/strategies/voxel_sph_strategy.py:65-107: GPU hash, copy to the
 // host, numpy structured sort by (voxel_id, particle_id), Python loop building
 // voxel_begin) with four device passes:
-//   1. hash: voxel id per particle + atomic histogram (slot = arrival rank);
+//   1. hash: voxel id per particle + atomic histogram (slot = arrival rank;
+//      one atomic per run of lanes in the same voxel);
 //   2. scan: exclusive prefix of the histogram = voxel_start (tile sums, one
 //      scan of the tile sums, tile-local warp-shuffle scans);
 //   3. scatter: particle id of each particle to voxel_start + slot;
@@ -63,20 +64,39 @@ k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
              int n, const float4* __restrict__ pos, int32_t* __restrict__ cell,
              int32_t* __restrict__ slot, int32_t* __restrict__ vcount) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
-    const float4 p = __ldg(pos + s);
-    int vid;
-    if (finite3(p)) {
-        const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
-        const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
-        const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
-        vid = sc.v_begin + voxel_index(vx, vy, vz, sc.tiled, sc.dims[0], sc.dims[1], sc.nt0, sc.nt1);
-    } else {
-        vid = sc.v_begin + sc.v_count;   // overflow bucket
+    const int lane = threadIdx.x & 31;
+    const bool valid = s < n;
+    int vid = -1;
+    if (valid) {
+        const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+        const float4 p = __ldg(pos + s);
+        if (finite3(p)) {
+            const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
+            const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
+            const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
+            vid = sc.v_begin + voxel_index(vx, vy, vz, sc.tiled, sc.dims[0], sc.dims[1], sc.nt0, sc.nt1);
+            cell[s] = vid;
+        } else {
+            vid = sc.v_begin + sc.v_count;   // overflow bucket
+            cell[s] = ~vid;                  // negative: overflow bucket (no pid order needed)
+        }
     }
-    cell[s] = finite3(p) ? vid : ~vid;   // negative: overflow bucket (no pid order needed)
-    slot[s] = atomicAdd(vcount + vid, 1);
+    // Lanes of a run with the same voxel (sorted input holds whole voxels in
+    // consecutive slots) take consecutive slots with one atomic by the run's
+    // first lane.  Every lane of the warp takes part, in range or not.
+    const unsigned full = 0xffffffffu;
+    const int prev = __shfl_up_sync(full, vid, 1);
+    const unsigned heads = __ballot_sync(full, !valid || lane == 0 || prev != vid);
+    const unsigned le = (2u << lane) - 1u;
+    const int leader = 31 - __clz(heads & le);
+    int base = 0;
+    if (valid && leader == lane) {
+        const unsigned above = heads & ~le;
+        const int next = above ? __ffs(above) - 1 : 32;
+        base = atomicAdd(vcount + vid, next - lane);
+    }
+    base = __shfl_sync(full, base, leader);
+    if (valid) slot[s] = base + (lane - leader);
 }
 
 __global__ void __launch_bounds__(kScanThreads)
