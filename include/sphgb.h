@@ -19,7 +19,11 @@
  *  - Particle state on the device is FP32: position and velocity as float4
  *    (x, y, z, unused) per particle, density as float, particle ids as int32.
  *    Device state is kept in voxel-sorted order; d_pid[s] names the original
- *    particle at sorted slot s.
+ *    particle at sorted slot s.  The stage entry points sort by the
+ *    reference's row-major voxel ids; the context's own step may number the
+ *    voxels of sparse scenes in 4x4x4 tiles instead, so the slot order of a
+ *    bound state after sphgb_ctx_step is a permutation of that (same
+ *    particles, same results in original order, read through d_pid).
  */
 #ifndef SPHGB_H
 #define SPHGB_H
