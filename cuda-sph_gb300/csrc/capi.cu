@@ -97,7 +97,7 @@ struct SphgbCtx {
     float4* fin = nullptr;             // force inputs, 2 per particle (see launch_density)
     NbrList nbr;                     // neighbour list of the step (density -> force pass)
     int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
-    int32_t* big_count = nullptr;     // counters[0]: big voxels, counters[1]: density tasks
+    int32_t* big_count = nullptr;     // counters: [0] big voxels, [1] density tasks, [2] tasks taken
     int2* tasks = nullptr;             // (voxel, first slot) per run of <= 32 slots
     // bound (caller-owned) state
     float4* posA = nullptr;
@@ -488,7 +488,7 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                      cudaEvent_t* ev = nullptr, bool with_tasks = false) {
     cudaStream_t st = L.stream;
     if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * L.v_total, st));
-    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 2 * sizeof(int32_t), st));
+    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 3 * sizeof(int32_t), st));
     SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, scan_tiles(L.v_total)));
@@ -548,7 +548,7 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
     if (rc) return rc;
     if (c->density_variant == SPHGB_DENSITY_WARP)
         SPHGB_CUDA(launch_density_wc(L, c->posB, vel_s, c->vstart, c->vcount, c->rho, c->fin,
-                                     c->nbr, c->tasks, c->big_count + 1));
+                                     c->nbr, c->tasks, c->big_count + 1, c->big_count + 2));
     else
         SPHGB_CUDA(launch_density(L, c->posB, vel_s, c->vstart, c->vcount, c->rho, c->fin,
                                   c->nbr));
@@ -639,7 +639,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     rc = rc ? rc : ensure(&c->pidB, k.pidB, N);
     rc = rc ? rc : ensure(&c->fin, k.fin, 2 * N);
     rc = rc ? rc : ensure(&c->big_list, k.big_list, N / kMinBigVoxel + 1);
-    rc = rc ? rc : ensure(&c->big_count, k.big_count, 2);
+    rc = rc ? rc : ensure(&c->big_count, k.big_count, 3);
     rc = rc ? rc : ensure(&c->tasks, k.tasks, N);
     rc = rc ? rc : ensure(&c->nbr.idx, k.nbr_idx, (size_t)kListCap * N);
     rc = rc ? rc : ensure(&c->nbr.count, k.nbr_count, N);

@@ -440,11 +440,12 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
 cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel,
                            const int32_t* vstart, const int32_t* vcount, float* rho,
                            float4* fin, NbrList nbr);
-// the step's density pass: one warp per task (<= 32 particles of one voxel)
+// the step's density pass: one warp per task (<= 32 particles of one voxel);
+// task_next: a zeroed counter from which the warps take the tasks
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
-                              const int32_t* task_count);
+                              const int32_t* task_count, int32_t* task_next);
 cudaError_t launch_gather_vel(const Launch& L, const int32_t* pid, const float4* vel_in,
                               const float* rho, float4* vel_out, float4* fin);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
