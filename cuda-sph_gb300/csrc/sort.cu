@@ -6,8 +6,9 @@
 // voxel_begin) with four device passes:
 //   1. hash: voxel id per particle + atomic histogram (slot = arrival rank;
 //      one atomic per run of lanes in the same voxel);
-//   2. scan: exclusive prefix of the histogram = voxel_start (tile sums, one
-//      scan of the tile sums, tile-local warp-shuffle scans);
+//   2. scan: exclusive prefix of the histogram = voxel_start (tile sums; each
+//      tile adds up the sums before it, or one block scans them for large
+//      tables; tile-local warp-shuffle scans);
 //   3. scatter: particle id of each particle to voxel_start + slot;
 //   4. rank-gather: each particle's final slot = voxel_start + number of
 //      members of its voxel with a smaller particle id; the state is gathered
@@ -144,6 +145,29 @@ k_scan_tile_sums(int32_t* __restrict__ tile_sums, int n_tiles) {
     }
 }
 
+// Tables of at most this many tiles skip the one-block scan of the tile sums:
+// each block of k_tile_scan adds up the sums of the tiles before it instead
+// (at most kScanDirectTiles / kScanThreads loads per thread).
+constexpr int kScanDirectTiles = 8192;
+
+// sum of tile_sums[0 .. n) over the block (every thread gets it)
+__device__ __forceinline__ int block_sum_before(const int32_t* __restrict__ tile_sums, int n) {
+    __shared__ int ws[kScanThreads / 32];
+    int v = 0;
+    for (int i = threadIdx.x; i < n; i += kScanThreads) v += __ldg(tile_sums + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int s = 0;
+#pragma unroll
+    for (int w = 0; w < kScanThreads / 32; ++w) s += ws[w];
+    return s;
+}
+
+// tile_prefix: the exclusive scan of the tile sums, or (direct) the tile sums
+// themselves, this block adding up those before it
+template <bool kDirect>
 __global__ void __launch_bounds__(kScanThreads)
 k_tile_scan(const int32_t* __restrict__ vcount, int v_total, const int32_t* __restrict__ tile_prefix,
             int32_t* __restrict__ vstart) {
@@ -165,7 +189,9 @@ k_tile_scan(const int32_t* __restrict__ vcount, int v_total, const int32_t* __re
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) tsum += v[i];
     int total = 0;
-    int run = block_excl_scan(tsum, total) + __ldg(tile_prefix + blockIdx.x);
+    const int before = kDirect ? block_sum_before(tile_prefix, blockIdx.x)
+                               : __ldg(tile_prefix + blockIdx.x);
+    int run = block_excl_scan(tsum, total) + before;
     int out[kScanItems];
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) { out[i] = run; run += v[i]; }
@@ -308,8 +334,14 @@ cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
                         int32_t* tile_sums, int n_tiles) {
     if (L.v_total == 0) return cudaSuccess;
     k_tile_reduce<<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums);
-    k_scan_tile_sums<<<1, kScanThreads, 0, L.stream>>>(tile_sums, n_tiles);
-    k_tile_scan<<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums, vstart);
+    if (n_tiles <= kScanDirectTiles) {
+        k_tile_scan<true><<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums,
+                                                                   vstart);
+    } else {
+        k_scan_tile_sums<<<1, kScanThreads, 0, L.stream>>>(tile_sums, n_tiles);
+        k_tile_scan<false><<<n_tiles, kScanThreads, 0, L.stream>>>(vcount, L.v_total, tile_sums,
+                                                                    vstart);
+    }
     return cudaGetLastError();
 }
 
