@@ -52,7 +52,10 @@ for _p in (os.path.join(ROOT, "cuda-sph_gb300"), ROOT):
 STAGE_BYTES_PER_PARTICLE = {"hash": 20, "scan": 0, "scatter": 8, "rank_gather": 48,
                             "density": 16, "force_integrate": 100, "step_counter": 0}
 STAGE_BYTES_PER_VOXEL = {"hash": 4, "scan": 8}
-KERNELS_PER_STEP = 10  # hash, 3 scan, scatter, big-voxel sort, rank-gather, density, force+integrate, counter
+# kernels per step: hash, scan (2; 3 for voxel tables over 8192 x 4096 entries),
+# scatter, big-voxel sort, rank-gather, density, force+integrate, step counter
+def kernels_per_step(n_voxels):
+    return 9 if (n_voxels + 4095) // 4096 <= 8192 else 10
 
 
 _T0 = time.perf_counter()
@@ -366,7 +369,7 @@ def run_gb300(args):
            "autotune": {"chosen": {"density": {0: "warp", 1: "thread"}[best.density_variant],
                                    "sort_block": best.sort_block, "big_voxel": best.big_voxel},
                         "ms_per_step": summary(tried)},
-           "clocks": clocks, "gpu_launches": KERNELS_PER_STEP * args.steps}
+           "clocks": clocks, "gpu_launches": kernels_per_step(batch.n_voxels) * args.steps}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"], want = cpu_baseline(spec, state, max(args.cpu_steps, 1))
         log(f"cpu baseline: {out['cpu_baseline']}")
