@@ -375,10 +375,34 @@ __device__ inline void pipe_collide(double* p, double* v, const PipeView& P, uin
     }
 }
 
+// ---- 256-bit global accesses ----------------------------------------------
+// One thread moves 32 bytes with one instruction (sm_100 and later; the
+// address must be 32-byte aligned).  In a gather, where the lanes of a warp
+// touch unrelated lines, an L1 pass costs per line touched, so one 32-byte
+// load of a force record costs half of two 16-byte loads.
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+__device__ __forceinline__ void ldg256(const int32_t* p, int (&v)[8]) {
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7])
+        : "l"(p));
+}
+__device__ __forceinline__ void stg256(float4* p, const float4& a, const float4& b) {
+    asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                 :: "l"(p), "f"(a.x), "f"(a.y), "f"(a.z), "f"(a.w), "f"(b.x), "f"(b.y),
+                    "f"(b.z), "f"(b.w)
+                 : "memory");
+}
+
 // ---- neighbour list --------------------------------------------------------
 // Neighbours (other than self) of every particle in walk order, recorded by
 // the density pass and read by the force pass.  One row per particle:
-// idx[s * kListCap + k].
+// idx[s * kListCap + k]; rows are 128-byte aligned (idx from cudaMalloc), so
+// the force pass reads a row eight entries per load.
 constexpr int kListCap = 32;
 struct NbrList {
     int32_t* idx = nullptr;     // kListCap * n entries

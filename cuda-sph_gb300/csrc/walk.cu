@@ -33,10 +33,12 @@ __device__ __forceinline__ void write_force_inputs(int s, const float4& pi, cons
                                                    const float4* __restrict__ vel, float r,
                                                    float4* __restrict__ fin) {
     const float p = sc.k * (r - sc.rho0);
-    fin[2 * s] = make_float4(pi.x, pi.y, pi.z, p / (r * r));
+    const float4 a = make_float4(pi.x, pi.y, pi.z, p / (r * r));
     if (vel) {
         const float4 v = __ldg(vel + s);
-        fin[2 * s + 1] = make_float4(v.x, v.y, v.z, 1.0f / r);
+        stg256(fin + 2 * s, a, make_float4(v.x, v.y, v.z, 1.0f / r));
+    } else {
+        fin[2 * s] = a;
     }
 }
 
@@ -503,7 +505,8 @@ __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
     walk(pi, geom, vstart, vcount, pos, geom.cap, [&](int j, float dx, float dy, float dz, float d2) {
         if (j == s) return;
-        const float4 a = __ldg(fin + 2 * j), b = __ldg(fin + 2 * j + 1);
+        float4 a, b;
+        ldg256(fin + 2 * j, a, b);
         add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(a.w, b.w), b, dx, dy, dz, d2);
     });
 }
@@ -518,16 +521,17 @@ __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& 
                                                 ForceSums<kPlain>& f) {
     const float inv_h = 1.0f / sc.h;
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
-    // the row is 16-byte aligned: four entries per load
-    for (int k0 = 0; k0 < cnt; k0 += 4) {
-        const int4 q = __ldg(reinterpret_cast<const int4*>(list) + (k0 >> 2));
-        const int js[4] = {q.x, q.y, q.z, q.w};
+    // eight list entries per load, one 32-byte load per neighbour record:
+    // this pass is a gather bound by L1 passes per line touched
+    for (int k0 = 0; k0 < cnt; k0 += 8) {
+        int js[8];
+        ldg256(list + k0, js);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < 8; ++u) {
             if (k0 + u >= cnt) break;
             const int j = js[u];
-            const float4 pj = __ldg(fin + 2 * j);       // position, p/rho^2
-            const float4 vj = __ldg(fin + 2 * j + 1);   // velocity, 1/rho
+            float4 pj, vj;                      // position, p/rho^2; velocity, 1/rho
+            ldg256(fin + 2 * j, pj, vj);
             const float dx = __fsub_rn(pi.x, pj.x);
             const float dy = __fsub_rn(pi.y, pj.y);
             const float dz = __fsub_rn(pi.z, pj.z);
@@ -592,7 +596,9 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
     const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
     const float4 pi = __ldg(pos + s);
     const float4 vi = __ldg(vel + s);
-    const float2 ai = make_float2(__ldg(fin + 2 * s).w, __ldg(fin + 2 * s + 1).w);
+    float4 fa, fb;
+    ldg256(fin + 2 * s, fa, fb);
+    const float2 ai = make_float2(fa.w, fb.w);
     const Forces f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, nullptr, n, -1);
     const float vscale = sc.mass * sc.visc * ai.y;
     pressure[s] = make_float4(f.p[0], f.p[1], f.p[2], 0.0f);
@@ -631,7 +637,9 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const SceneDev& sc = scenes[si];
     const float4 pi = __ldg(pos + s);
     const float4 vi = __ldg(vel + s);
-    const float2 ai = make_float2(__ldg(fin + 2 * s).w, __ldg(fin + 2 * s + 1).w);
+    float4 fa, fb;
+    ldg256(fin + 2 * s, fa, fb);
+    const float2 ai = make_float2(fa.w, fb.w);
     const float rho_i = __ldg(rho + s);
     const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
     const Forces f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount,
