@@ -373,23 +373,38 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         __syncwarp();
         // (a) one lane per list entry: the density term of every accepted pair
         // replaces the entry (self gets kSelfTerm), and each particle's list
-        // row (neighbours other than itself, walk order) is written coalesced
+        // row (neighbours other than itself, walk order) is written coalesced.
+        // Two particles' rows at a time, their position gathers issued together.
         const float inv_h2 = 1.0f / sc.h2;
-        for (int i = 0; i < c_t; ++i) {
-            const int na_i = min(__shfl_sync(full, cnt, i), cap);
-            const int si = d0 + i;
-            const bool in = lane < na_i;
-            const int j = in ? S.list[i][lane] : -1;
-            const unsigned self = __ballot_sync(full, in && j == si);
-            if (in) {
-                int term = kSelfTerm;
-                if (j != si) {
-                    const float d2 = dist2(S.home[i], __ldg(pos + j));
-                    const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-                    term = __float_as_int(u * u * u);
-                    if (nbr.idx) nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
+        for (int i0 = 0; i0 < c_t; i0 += 2) {
+            int jj[2];
+            float4 pq[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int i = i0 + e;   // i0 even and < c_t <= 32: i <= 31
+                const int na_i = i < c_t ? min(__shfl_sync(full, cnt, i), cap) : 0;
+                jj[e] = lane < na_i ? S.list[i][lane] : -1;
+                pq[e] = jj[e] >= 0 ? __ldg(pos + jj[e]) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int i = i0 + e;
+                if (i >= c_t) break;
+                const int si = d0 + i;
+                const int j = jj[e];
+                const bool in = j >= 0;
+                const unsigned self = __ballot_sync(full, in && j == si);
+                if (in) {
+                    int term = kSelfTerm;
+                    if (j != si) {
+                        const float d2 = dist2(S.home[i], pq[e]);
+                        const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                        term = __float_as_int(u * u * u);
+                        if (nbr.idx)
+                            nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
+                    }
+                    S.list[i][lane] = term;
                 }
-                S.list[i][lane] = term;
             }
         }
         __syncwarp();
