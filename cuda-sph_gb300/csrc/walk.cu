@@ -536,24 +536,33 @@ __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& 
                                                 ForceSums<kPlain>& f) {
     const float inv_h = 1.0f / sc.h;
     const float gw = sc.grad_w_const, lw = sc.lap_w_const;
-    // eight list entries per load, one 32-byte load per neighbour record:
-    // this pass is a gather bound by L1 passes per line touched
+    // Eight list entries per load, one 32-byte load per neighbour record:
+    // this pass is a gather bound by L1 passes per line touched, and by load
+    // latency.  Records are loaded two at a time ahead of their arithmetic (the
+    // second, past the end of the list, reloads the first).
     for (int k0 = 0; k0 < cnt; k0 += 8) {
         int js[8];
         ldg256(list + k0, js);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            if (k0 + u >= cnt) break;
-            const int j = js[u];
-            float4 pj, vj;                      // position, p/rho^2; velocity, 1/rho
-            ldg256(fin + 2 * j, pj, vj);
-            const float dx = __fsub_rn(pi.x, pj.x);
-            const float dy = __fsub_rn(pi.y, pj.y);
-            const float dz = __fsub_rn(pi.z, pj.z);
-            float d2 = __fmul_rn(dx, dx);
-            d2 = __fmaf_rn(dy, dy, d2);
-            d2 = __fmaf_rn(dz, dz, d2);
-            add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(pj.w, vj.w), vj, dx, dy, dz, d2);
+        for (int u0 = 0; u0 < 8; u0 += 2) {
+            if (k0 + u0 >= cnt) break;
+            float4 pq[2], vq[2];                // position, p/rho^2; velocity, 1/rho
+            ldg256(fin + 2 * js[u0], pq[0], vq[0]);
+            ldg256(fin + 2 * (k0 + u0 + 1 < cnt ? js[u0 + 1] : js[u0]), pq[1], vq[1]);
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                if (k0 + u0 + e >= cnt) break;
+                const float4& pj = pq[e];
+                const float4& vj = vq[e];
+                const float dx = __fsub_rn(pi.x, pj.x);
+                const float dy = __fsub_rn(pi.y, pj.y);
+                const float dz = __fsub_rn(pi.z, pj.z);
+                float d2 = __fmul_rn(dx, dx);
+                d2 = __fmaf_rn(dy, dy, d2);
+                d2 = __fmaf_rn(dz, dz, d2);
+                add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(pj.w, vj.w), vj, dx, dy, dz,
+                         d2);
+            }
         }
     }
 }
