@@ -55,7 +55,11 @@ STAGE_BYTES_PER_VOXEL = {"hash": 4, "scan": 8}
 # kernels per step: hash, scan (2; 3 for voxel tables over 8192 x 4096 entries),
 # scatter, big-voxel sort, rank-gather, density, force+integrate, step counter
 def kernels_per_step(n_voxels):
-    return 9 if (n_voxels + 4095) // 4096 <= 8192 else 10
+    """Our kernels per fused step of a box context: hash, tile reduce, tile
+    scan (plus the one-block scan of the tile sums above 8192 tiles), scatter,
+    big-voxel sort, rank-gather, density, the force pass's two launches (the
+    list path, then the deferred particles) and the step counter."""
+    return 10 if (n_voxels + 4095) // 4096 <= 8192 else 11
 
 
 _T0 = time.perf_counter()

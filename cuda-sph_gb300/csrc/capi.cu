@@ -63,6 +63,9 @@ constexpr double kTileMaxOccupancy = 8.0;   // particles per voxel, table mean
 constexpr int kHostRanges = 8;
 constexpr int kHostFirstRangeEvent = 6;
 constexpr int kHostEvents = kHostFirstRangeEvent + kHostRanges;
+// device counters in big_count: big voxels, density tasks, tasks taken, then the
+// deferred particles of the whole force pass and of each host-entry range
+constexpr int kCounters = 4 + kHostRanges;
 
 struct SphgbCtx {
     int device = 0;
@@ -97,7 +100,9 @@ struct SphgbCtx {
     float4* fin = nullptr;             // force inputs, 2 per particle (see launch_density)
     NbrList nbr;                     // neighbour list of the step (density -> force pass)
     int32_t* big_list = nullptr;     // voxels with more than kBigVoxel members
-    int32_t* big_count = nullptr;     // counters: [0] big voxels, [1] density tasks, [2] tasks taken
+    int32_t* big_count = nullptr;     // counters: [0] big voxels, [1] density tasks, [2] tasks taken,
+                                      // [3 + r] deferred particles of force pass r (kCounters)
+    int32_t* rare = nullptr;          // deferred particles of the force pass (RareList)
     int2* tasks = nullptr;             // (voxel, first slot) per run of <= 32 slots
     // bound (caller-owned) state
     float4* posA = nullptr;
@@ -125,7 +130,7 @@ struct SphgbCtx {
         size_t scenes = 0, scenes_ref = 0, pbegin = 0, pipe = 0, cell = 0, slot_of = 0, slot = 0, tmp_pid = 0,
                vstart = 0,
                vcount = 0, tile_sums = 0, posB = 0, velB = 0, pidB = 0, fin = 0, big_list = 0,
-               big_count = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
+               big_count = 0, rare = 0, tasks = 0, nbr_idx = 0, nbr_count = 0, pos64B = 0, chunks = 0,
                partials = 0;
     } cap;
     // tuning (sphgb_ctx_set_tuning)
@@ -182,7 +187,7 @@ void free_ctx(SphgbCtx* c) {
     void* ptrs[] = {c->d_scenes, c->d_scenes_ref, c->d_pbegin, c->d_pipe, c->cell, c->slot_of, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->fin, c->owned, c->stage, c->d_chunks, c->d_partials,
-                    c->big_list, c->big_count, c->nbr.idx, c->nbr.count, c->tasks};
+                    c->big_list, c->big_count, c->rare, c->nbr.idx, c->nbr.count, c->tasks};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -488,7 +493,7 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
                      cudaEvent_t* ev = nullptr, bool with_tasks = false) {
     cudaStream_t st = L.stream;
     if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * L.v_total, st));
-    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, 3 * sizeof(int32_t), st));
+    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, kCounters * sizeof(int32_t), st));
     SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, scan_tiles(L.v_total)));
@@ -507,21 +512,27 @@ int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const floa
 // force + integrate + wall pass of the step (after the density pass), over
 // all slots, or over a range of particles in original order when range is
 // given (see PidRange)
-int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range) {
+int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range, int range_index) {
     const bool sep = c->out_pos != nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
     float4* pos_o = sep ? c->out_pos : c->posA;
     float4* vel_o = sep ? c->out_vel : c->velA;
     int32_t* pid_o = sep ? c->out_pid : c->pidA;
     double* p64_o = c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr;
+    // deferred particles: pass r of the host entry counts in big_count[4 + r]
+    // and lists rows of its range from range->i0; the whole pass in [3] from 0
+    RareList rare;
+    rare.idx = c->rare;
+    rare.count = c->big_count + 3 + (range ? 1 + range_index : 0);
+    rare.base = range ? range->i0 : 0;
     if (range)
         SPHGB_CUDA(launch_integrate_range(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B,
                                           c->vstart, c->vcount, c->scene_step, c->nbr, pos_o,
-                                          vel_o, pid_o, p64_o, *range));
+                                          vel_o, pid_o, p64_o, *range, rare));
     else
         SPHGB_CUDA(launch_integrate(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B, c->vstart,
                                     c->vcount, c->scene_step, c->nbr, pos_o, vel_o, pid_o, p64_o,
-                                    nullptr));
+                                    nullptr, rare));
     return SPHGB_OK;
 }
 
@@ -559,7 +570,7 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
         SPHGB_CUDA(launch_gather_vel(L, c->pidB, c->velA, c->rho, c->velB, c->fin));
     }
     if (!with_forces) return SPHGB_OK;
-    rc = enqueue_forces(c, L, nullptr);
+    rc = enqueue_forces(c, L, nullptr, 0);
     if (rc) return rc;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[6], st));
     k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
@@ -639,7 +650,8 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     rc = rc ? rc : ensure(&c->pidB, k.pidB, N);
     rc = rc ? rc : ensure(&c->fin, k.fin, 2 * N);
     rc = rc ? rc : ensure(&c->big_list, k.big_list, N / kMinBigVoxel + 1);
-    rc = rc ? rc : ensure(&c->big_count, k.big_count, 3);
+    rc = rc ? rc : ensure(&c->big_count, k.big_count, kCounters);
+    rc = rc ? rc : ensure(&c->rare, k.rare, N);
     rc = rc ? rc : ensure(&c->tasks, k.tasks, N);
     rc = rc ? rc : ensure(&c->nbr.idx, k.nbr_idx, (size_t)kListCap * N);
     rc = rc ? rc : ensure(&c->nbr.count, k.nbr_count, N);
@@ -1032,7 +1044,7 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
             range.i1 = (int)(N * (r + 1) / kHostRanges);
             range.pos = sp;
             range.vel = sv;
-            rc = enqueue_forces(ctx, L, &range);
+            rc = enqueue_forces(ctx, L, &range, r);
             if (rc) return rc;
             SPHGB_CUDA(cudaEventRecord(ctx->host_ev[kHostFirstRangeEvent + r], st));
             SPHGB_CUDA(cudaStreamWaitEvent(st2, ctx->host_ev[kHostFirstRangeEvent + r], 0));

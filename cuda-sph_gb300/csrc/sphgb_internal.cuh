@@ -420,6 +420,16 @@ struct PidRange {
     double* vel = nullptr;      // (n, 3) FP64
 };
 
+// Particles a lean force pass defers to a second launch (see kForceLean in
+// walk.cu): entries idx[base + k] for k < *count, each a slot, or a row of
+// the PidRange in range mode.  Unset (count null): one pass does every
+// particle.
+struct RareList {
+    int32_t* idx = nullptr;
+    int32_t* count = nullptr;   // zeroed before the pass
+    int base = 0;
+};
+
 // ---- launchers (host) -----------------------------------------------------
 struct Launch {
     const SceneDev* scenes;     // device array
@@ -480,13 +490,14 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
-                             float4* force_out);
+                             float4* force_out, RareList rare = RareList{});
 cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const float4* vel,
                                    const float* rho, const float4* fin, const int32_t* pid,
                                    const double* pos64, const int32_t* vstart,
                                    const int32_t* vcount, const int32_t* scene_step, NbrList nbr,
                                    float4* pos_out, float4* vel_out, int32_t* pid_out,
-                                   double* pos64_out, PidRange range);
+                                   double* pos64_out, PidRange range,
+                                   RareList rare = RareList{});
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,
                               const int32_t* vcount, int32_t* list, int stride,
                               int32_t* n_capped, int32_t* n_uncapped);

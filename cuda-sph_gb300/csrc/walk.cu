@@ -630,14 +630,25 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
                                visc_term(f, 2, vscale), 0.0f);
 }
 
+// Modes of the force pass.  kForceAll: every particle, every path.  The
+// list path alone (the neighbour list, finite factors, Kahan sums) needs far
+// fewer registers than the walk fallback and the plain re-sum, whose spills
+// slowed it; so a pass with a neighbour list runs as kForceLean, which
+// appends each particle needing a rare path to a RareList and writes nothing
+// for it, followed by kForceRare, a small grid-stride launch over those
+// particles with every path.  The per-particle arithmetic is the same in all
+// three: the results are identical.
+constexpr int kForceAll = 0, kForceLean = 1, kForceRare = 2;
+constexpr int kRareBlocks = 152;   // kForceRare grid (one block per SM)
+
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
 // (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
 // state into the *_out buffers at the same slot.  kPipe = false is the
 // instantiation for contexts without pipe scenes (no FP64 code).  kRange:
 // one thread per particle of range.i0..i1 in original order (same per-particle
 // arithmetic), which also writes the FP64 rows of the next position and
-// velocity.
-template <bool kPipe, bool kRange>
+// velocity.  kMode: see kForceAll.
+template <bool kPipe, bool kRange, int kMode>
 __global__ void __launch_bounds__(kBlock, kPipe ? 1 : 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
@@ -647,14 +658,20 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
             NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
-            float4* __restrict__ force_out, PidRange range) {
+            float4* __restrict__ force_out, PidRange range, RareList rare) {
+    const int m_rare = kMode == kForceRare ? *rare.count : 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
     int s, row = 0;
-    if (kRange) {
-        row = range.i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (kMode == kForceRare) {
+        if (k >= m_rare) return;
+        row = rare.idx[rare.base + k];
+        s = kRange ? __ldg(range.slot_of + row) : row;
+    } else if (kRange) {
+        row = range.i0 + k;
         if (row >= range.i1) return;
         s = __ldg(range.slot_of + row);
     } else {
-        s = blockIdx.x * blockDim.x + threadIdx.x;
+        s = k;
         if (s >= n) return;
     }
     const int si = scene_of(s, pbegin, n_scenes);
@@ -666,8 +683,23 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     const float2 ai = make_float2(fa.w, fb.w);
     const float rho_i = __ldg(rho + s);
     const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
-    const Forces f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount,
-                               nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr, n, cnt);
+    const int32_t* list = nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr;
+    Forces f;
+    if (kMode == kForceLean) {
+        ForceSums<false> fs;
+        bool ok = cnt >= 0 && fabsf(ai.x * ai.y) < INFINITY;
+        if (ok) {
+            force_sums_list<false>(pi, vi, ai.x, sc, fin, list, n, cnt, fs);
+            ok = !fs.bad;
+        }
+        if (!ok) {
+            rare.idx[rare.base + atomicAdd(rare.count, 1)] = kRange ? row : s;
+            return;
+        }
+        f = Forces{{fs.px.s, fs.py.s, fs.pz.s}, {fs.vx.s, fs.vy.s, fs.vz.s}, fs.terms};
+    } else {
+        f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, list, n, cnt);
+    }
     const float vscale = sc.mass * sc.visc * ai.y;
     // result_force = ext + -P + V (base_kernels.py:46-52)
     float F[3];
@@ -724,6 +756,8 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     }
     pid_out[s] = p_id;
     if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
+    if (kMode != kForceRare) return;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -803,22 +837,51 @@ cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,
     return cudaGetLastError();
 }
 
+namespace {
+// the force pass of one launch shape: with a neighbour list and a RareList
+// (contexts without pipe scenes), the lean pass then the deferred particles;
+// otherwise every particle in one pass
+template <bool kRange>
+cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const float4* vel,
+                              const float* rho, const float4* fin, const int32_t* pid,
+                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
+                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
+                              float4* vel_out, int32_t* pid_out, double* pos64_out,
+                              float4* force_out, PidRange range, RareList rare) {
+    if (L.pipe_scenes) {
+        k_integrate<true, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
+            RareList{});
+    } else if (nbr.count && rare.count) {
+        k_integrate<false, kRange, kForceLean><<<blocks_for(m), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_integrate<false, kRange, kForceRare><<<kRareBlocks, kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
+    } else {
+        k_integrate<false, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
+            RareList{});
+    }
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* vel,
                              const float* rho, const float4* fin, const int32_t* pid,
                              const double* pos64, const int32_t* vstart, const int32_t* vcount,
                              const int32_t* scene_step, NbrList nbr, float4* pos_out,
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
-                             float4* force_out) {
+                             float4* force_out, RareList rare) {
     if (L.n == 0) return cudaSuccess;
-    if (L.pipe_scenes)
-        k_integrate<true, false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, PidRange{});
-    else
-        k_integrate<false, false><<<blocks_for(L.n), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, PidRange{});
-    return cudaGetLastError();
+    return launch_force_pass<false>(L, L.n, pos, vel, rho, fin, pid, pos64, vstart, vcount,
+                                    scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
+                                    force_out, PidRange{}, rare);
 }
 
 cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const float4* vel,
@@ -826,20 +889,14 @@ cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const flo
                                    const double* pos64, const int32_t* vstart,
                                    const int32_t* vcount, const int32_t* scene_step, NbrList nbr,
                                    float4* pos_out, float4* vel_out, int32_t* pid_out,
-                                   double* pos64_out, PidRange range) {
+                                   double* pos64_out, PidRange range, RareList rare) {
     const int m = range.i1 - range.i0;
     if (m <= 0) return cudaSuccess;
     if (range.i0 < 0 || range.i1 > L.n || !range.slot_of || !range.pos || !range.vel)
         return cudaErrorInvalidValue;
-    if (L.pipe_scenes)
-        k_integrate<true, true><<<blocks_for(m), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, nullptr, range);
-    else
-        k_integrate<false, true><<<blocks_for(m), kBlock, 0, L.stream>>>(
-            L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, nullptr, range);
-    return cudaGetLastError();
+    return launch_force_pass<true>(L, m, pos, vel, rho, fin, pid, pos64, vstart, vcount,
+                                   scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
+                                   nullptr, range, rare);
 }
 
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,

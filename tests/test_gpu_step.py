@@ -18,13 +18,19 @@ def _scenes():
         "uncapped": scenes.box_dam_break(nx=10, ny=20, nz=10, max_neighbours=0, seed=4),
         "truncated": scenes.box_dam_break(nx=10, ny=20, nz=10, box=(0.7, 0.7, 0.7),
                                           walk_dims='truncated', seed=5),
+        # lattice spacing above h: about one particle in five has no neighbour,
+        # density 0 and non-finite force factors, so the force pass defers it
+        # to its second launch (the plain re-sum)
+        "sparse": scenes.box_dam_break(nx=8, ny=8, nz=8, spacing=0.05, jitter=0.01, seed=6),
     }
 
 
-@pytest.mark.parametrize("name", ["config0", "pipe", "uncapped", "truncated"])
+@pytest.mark.parametrize("name", ["config0", "pipe", "uncapped", "truncated", "sparse"])
 def test_fused_step_bit_identical_to_stages(name):
     """The fused step reads the density pass's neighbour list; the stage path
-    walks again.  Same neighbours, order and arithmetic: identical bits."""
+    walks again.  Same neighbours, order and arithmetic: identical bits.  The
+    uncapped and sparse scenes send particles through the force pass's second
+    launch (a walk, the plain re-sum); the stage path has one launch."""
     torch_cuda()
     from sphgb.device import SceneBatch
     spec, st = _scenes()[name]
@@ -101,7 +107,7 @@ def test_host_entry_matches_oracle():
 
 
 @pytest.mark.parametrize("order", ["slot", "particle", "auto"])
-@pytest.mark.parametrize("name", ["config0", "pipe"])
+@pytest.mark.parametrize("name", ["config0", "pipe", "sparse"])
 def test_host_entry_bit_identical_to_device_path(name, order):
     """Calls of sphgb_compute_next_state_host in a row (uploads and downloads
     spread over two streams; the force pass in slot order, in particle-order
