@@ -62,7 +62,12 @@ constexpr int64_t kMaxParticles = SPHGB_MAX_PARTICLES;
 constexpr double kTileMaxOccupancy = 8.0;   // particles per voxel, table mean
 constexpr int kHostRanges = 8;
 constexpr int kHostFirstRangeEvent = 6;
-constexpr int kHostEvents = kHostFirstRangeEvent + kHostRanges;
+// the host entry uploads the positions in kHostPosChunks parts; each is
+// converted and hashed while the next one is in flight
+constexpr int kHostPosChunks = 4;
+constexpr int kHostFirstChunkEvent = kHostFirstRangeEvent + kHostRanges;
+constexpr int kHostOrganizedEvent = kHostFirstChunkEvent + kHostPosChunks;
+constexpr int kHostEvents = kHostOrganizedEvent + 1;
 // device counters in big_count: big voxels, density tasks, tasks taken, then the
 // deferred particles of the whole force pass and of each host-entry range
 constexpr int kCounters = 4 + kHostRanges;
@@ -289,12 +294,14 @@ int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d,
     return SPHGB_OK;
 }
 
+// rows i0..n-1 of an FP64 AoS state into the float4 state (and the pipe
+// accumulator); vel or pos may be null
 __global__ void k_load_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
-                           int n_scenes, int n, const double* __restrict__ pos,
+                           int n_scenes, int i0, int n, const double* __restrict__ pos,
                            const double* __restrict__ vel, float4* __restrict__ pos_out,
                            float4* __restrict__ vel_out, int32_t* __restrict__ pid_out,
                            double* __restrict__ pos64_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (vel)
         vel_out[i] = make_float4((float)vel[3 * i], (float)vel[3 * i + 1], (float)vel[3 * i + 2], 0.0f);
@@ -490,11 +497,13 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 int enqueue_organize(SphgbCtx* c, const Launch& L, const float4* pos, const float4* vel,
                      const int32_t* pid, const double* pos64, float4* pos_o, float4* vel_o,
                      int32_t* pid_o, double* pos64_o, int32_t* vstart, int32_t* vcount,
-                     cudaEvent_t* ev = nullptr, bool with_tasks = false) {
+                     cudaEvent_t* ev = nullptr, bool with_tasks = false, bool hashed = false) {
     cudaStream_t st = L.stream;
-    if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * L.v_total, st));
-    SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, kCounters * sizeof(int32_t), st));
-    SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
+    if (!hashed) {   // else the caller cleared vcount and the counters and hashed every particle
+        if (L.v_total > 0) SPHGB_CUDA(cudaMemsetAsync(vcount, 0, sizeof(int32_t) * L.v_total, st));
+        SPHGB_CUDA(cudaMemsetAsync(c->big_count, 0, kCounters * sizeof(int32_t), st));
+        SPHGB_CUDA(launch_hash_count(L, pos, c->cell, c->slot, vcount));
+    }
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[0], st));
     SPHGB_CUDA(launch_scan(L, vcount, vstart, c->tile_sums, scan_tiles(L.v_total)));
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[1], st));
@@ -544,10 +553,13 @@ int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range, int rang
 // this event, brings them into slot order for the force pass.  density_done
 // (optional): recorded after the density pass.
 // with_forces = false stops after the density pass (and the velocity gather):
-// the caller then runs enqueue_forces itself and the step counter.
+// the caller then runs enqueue_forces itself and the step counter.  hashed:
+// the caller has cleared the histogram and the counters and hashed every
+// particle (in parts, as they arrived).  organized (optional): recorded once
+// the state is voxel-sorted.
 int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
                  cudaEvent_t vel_ready = nullptr, cudaEvent_t density_done = nullptr,
-                 bool with_forces = true) {
+                 bool with_forces = true, bool hashed = false, cudaEvent_t organized = nullptr) {
     const Launch L = c->launch(st);
     double* p64A = c->any_pipe ? c->pos64A : nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
@@ -555,8 +567,9 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
     const float4* vel_in = vel_ready ? nullptr : c->velA;   // null: gathered after density
     const float4* vel_s = vel_ready ? nullptr : c->velB;
     int rc = enqueue_organize(c, L, c->posA, vel_in, c->pidA, p64A, c->posB, c->velB, c->pidB,
-                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true);
+                              p64B, c->vstart, c->vcount, ev ? ev + 1 : nullptr, true, hashed);
     if (rc) return rc;
+    if (organized) SPHGB_CUDA(cudaEventRecord(organized, st));
     if (c->density_variant == SPHGB_DENSITY_WARP)
         SPHGB_CUDA(launch_density_wc(L, c->posB, vel_s, c->vstart, c->vcount, c->rho, c->fin,
                                      c->nbr, c->tasks, c->big_count + 1, c->big_count + 2));
@@ -836,7 +849,7 @@ int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double*
     if (!d_pos_aos || !d_vel_aos) return fail(SPHGB_ERR_INVALID, "null input");
     cudaStream_t st = as_stream(stream);
     k_load_aos<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes,
-                                                 ctx->n, d_pos_aos, d_vel_aos, ctx->posA,
+                                                 0, ctx->n, d_pos_aos, d_vel_aos, ctx->posA,
                                                  ctx->velA, ctx->pidA, ctx->pos64A);
     SPHGB_CUDA(cudaGetLastError());
     return SPHGB_OK;
@@ -974,46 +987,74 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
         }
     }
     cudaStream_t st = ctx->host_stream, st2 = ctx->host_stream2;
-    cudaEvent_t e_start = ctx->host_ev[0], e_pos = ctx->host_ev[1], e_vel = ctx->host_ev[2],
+    cudaEvent_t e_start = ctx->host_ev[0], e_vel = ctx->host_ev[2],
                 e_rho = ctx->host_ev[3], e_slot = ctx->host_ev[4], e_done = ctx->host_ev[5];
     double* sp = ctx->stage;
     double* sv = ctx->stage + 3 * N;
     double* sr = ctx->stage + 6 * N;
     const size_t b3 = sizeof(double) * 3 * N;
     const int nb = blocks(ctx->n);
-    // Two streams.  st: position upload and the step.  st2: the velocity
-    // upload, queued behind the position upload (they share the host link) so
-    // that the voxel sort and the density pass, which need positions only, run
-    // while it is in flight (the step gathers the velocities into slot order
-    // after the density pass); then, once the density pass is done, the
-    // density download, which overlaps the force pass.  The next positions and
+    // Two streams.  st2 uploads: the positions in kHostPosChunks parts, then
+    // the velocities.  st runs the step: each part of the positions is
+    // converted and hashed as soon as it is in (the voxel histogram fills in
+    // parts while the rest is in flight), then the voxel sort and the density
+    // pass, which need positions only, run while the velocities are still on
+    // the host link; the step gathers them into slot order after the density
+    // pass.  Once the state is voxel-sorted, st2 builds the map from
+    // original index to slot; once the density pass is done, it downloads the
+    // densities, which overlaps the force pass.  The next positions and
     // velocities are downloaded whole from st after the force pass (slot
     // order), or range by range from st2 while st computes the next range
     // (particle order).  Results are the same bits as the one-stream sequence.
     SPHGB_CUDA(cudaEventRecord(e_start, st));
     SPHGB_CUDA(cudaStreamWaitEvent(st2, e_start, 0));
-    SPHGB_CUDA(cudaMemcpyAsync(sp, h_pos, b3, cudaMemcpyHostToDevice, st));
-    SPHGB_CUDA(cudaEventRecord(e_pos, st));
-    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_pos, 0));
+    if (ctx->v_total > 0)
+        SPHGB_CUDA(cudaMemsetAsync(ctx->vcount, 0, sizeof(int32_t) * ctx->v_total, st));
+    SPHGB_CUDA(cudaMemsetAsync(ctx->big_count, 0, kCounters * sizeof(int32_t), st));
+    {
+        const Launch L = ctx->launch(st);
+        for (int k = 0; k < kHostPosChunks; ++k) {
+            // parts start on whole warps (the hash aggregates its atomics per warp)
+            auto bound = [&](int q) {
+                return (int)std::min(N, ((N * q / kHostPosChunks) + 31) & ~(size_t)31);
+            };
+            const int i0 = bound(k);
+            const int i1 = k + 1 == kHostPosChunks ? (int)N : bound(k + 1);
+            if (i1 <= i0) continue;
+            cudaEvent_t e_part = ctx->host_ev[kHostFirstChunkEvent + k];
+            SPHGB_CUDA(cudaMemcpyAsync(sp + 3 * (size_t)i0, h_pos + 3 * (size_t)i0,
+                                       sizeof(double) * 3 * (i1 - i0), cudaMemcpyHostToDevice,
+                                       st2));
+            SPHGB_CUDA(cudaEventRecord(e_part, st2));
+            SPHGB_CUDA(cudaStreamWaitEvent(st, e_part, 0));
+            k_load_aos<<<blocks(i1 - i0), kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin,
+                                                            ctx->n_scenes, i0, i1, sp, nullptr,
+                                                            ctx->posA, ctx->velA, ctx->pidA,
+                                                            ctx->pos64A);
+            SPHGB_CUDA(cudaGetLastError());
+            SPHGB_CUDA(launch_hash_count(L, ctx->posA, ctx->cell, ctx->slot, ctx->vcount, i0, i1));
+        }
+    }
     SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, b3, cudaMemcpyHostToDevice, st2));
-    k_load_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+    k_load_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n,
                                        nullptr, sv, ctx->posA, ctx->velA, ctx->pidA, nullptr);
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_vel, st2));
-    k_load_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sp,
-                                      nullptr, ctx->posA, ctx->velA, ctx->pidA, ctx->pos64A);
-    SPHGB_CUDA(cudaGetLastError());
     const int order = host_order_for_call(ctx);
     const auto t0 = std::chrono::steady_clock::now();
-    int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho, order == SPHGB_HOST_ORDER_SLOT);
+    cudaEvent_t e_org = ctx->host_ev[kHostOrganizedEvent];
+    int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho, order == SPHGB_HOST_ORDER_SLOT, true,
+                          e_org);
     if (rc) return rc;
     // st2: original index -> slot (from the sorted ids, which the force pass
-    // copies to the output unchanged), then the densities in original order
-    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
+    // copies to the output unchanged) during the density pass, then the
+    // densities in original order
+    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_org, 0));
     k_slot_of<<<nb, kBlock, 0, st2>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n, ctx->pidB,
                                       ctx->slot_of);
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_slot, st2));
+    SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
     k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                         nullptr, nullptr, ctx->rho, ctx->slot_of, nullptr,
                                         nullptr, nullptr, sr);

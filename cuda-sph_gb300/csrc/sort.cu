@@ -62,11 +62,11 @@ __device__ __forceinline__ int block_excl_scan(int v, int& total) {
 
 __global__ void __launch_bounds__(512)
 k_hash_count(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
-             int n, const float4* __restrict__ pos, int32_t* __restrict__ cell,
+             int i0, int i1, const float4* __restrict__ pos, int32_t* __restrict__ cell,
              int32_t* __restrict__ slot, int32_t* __restrict__ vcount) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = i0 + blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
-    const bool valid = s < n;
+    const bool valid = s < i1;
     int vid = -1;
     if (valid) {
         const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
@@ -322,11 +322,13 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
 int scan_tiles(int v_total) { return (v_total + kScanTile - 1) / kScanTile; }
 
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
-                              int32_t* vcount) {
-    if (L.n == 0) return cudaSuccess;
+                              int32_t* vcount, int i0, int i1) {
+    if (i1 < 0) i1 = L.n;
+    if (i0 < 0 || i1 > L.n || i0 > i1) return cudaErrorInvalidValue;
+    if (i1 == i0) return cudaSuccess;
     const int b = L.sort_block;
-    k_hash_count<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos,
-                                                        cell, slot, vcount);
+    k_hash_count<<<(i1 - i0 + b - 1) / b, b, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, i0,
+                                                            i1, pos, cell, slot, vcount);
     return cudaGetLastError();
 }
 

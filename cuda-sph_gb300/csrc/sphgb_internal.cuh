@@ -445,9 +445,12 @@ struct Launch {
     cudaStream_t stream;
 };
 
-// cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow bucket
+// cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow
+// bucket; slot[s] = its arrival slot in the voxel.  Particles i0..i1 (i1 < 0:
+// all): the histogram may be filled in several launches over parts of the state
+// (the arrival order inside a voxel is dropped by the rank-gather).
 cudaError_t launch_hash_count(const Launch& L, const float4* pos, int32_t* cell, int32_t* slot,
-                              int32_t* vcount);
+                              int32_t* vcount, int i0 = 0, int i1 = -1);
 cudaError_t launch_scan(const Launch& L, const int32_t* vcount, int32_t* vstart,
                         int32_t* tile_sums, int n_tiles);
 int scan_tiles(int v_total);
