@@ -654,7 +654,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     rc = rc ? rc : ensure(&c->cell, k.cell, N);
     rc = rc ? rc : ensure(&c->slot_of, k.slot_of, N);
     rc = rc ? rc : ensure(&c->slot, k.slot, N);
-    rc = rc ? rc : ensure(&c->tmp_pid, k.tmp_pid, N);
+    rc = rc ? rc : ensure(&c->tmp_pid, k.tmp_pid, N + 4);   // + 4: see k_rank_gather
     rc = rc ? rc : ensure(&c->vstart, k.vstart, V);
     rc = rc ? rc : ensure(&c->vcount, k.vcount, V);
     rc = rc ? rc : ensure(&c->tile_sums, k.tile_sums, (size_t)n_tiles);
@@ -1362,7 +1362,7 @@ struct NoAllocScratch {
     int32_t tile_sums[kNoAllocMaxTiles];
     int32_t cell[kNoAllocMaxParticles];
     int32_t slot[kNoAllocMaxParticles];
-    int32_t tmp_pid[kNoAllocMaxParticles];
+    alignas(16) int32_t tmp_pid[kNoAllocMaxParticles + 4];   // + 4: see k_rank_gather
     int32_t big_list[kNoAllocMaxParticles / kBigVoxel + 1];
 };
 

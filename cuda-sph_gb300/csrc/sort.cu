@@ -296,7 +296,15 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
     if (code < 0) {
         r = slot[s];                    // overflow bucket: arrival order, no pid order
     } else if (c <= big_voxel) {
-        for (int k = 0; k < c; ++k) r += __ldg(tmp_pid + st + k) < p;
+        // the voxel's ids four per load from the aligned quad at or before st;
+        // entries outside [st, st + c) are masked (tmp_pid is 16-byte aligned
+        // and padded by 4 entries, so the last quad stays inside it)
+        const int e = st + c;
+        for (int k = st & ~3; k < e; k += 4) {
+            const int4 q = __ldg(reinterpret_cast<const int4*>(tmp_pid + k));
+            r += (k >= st && q.x < p) + (k + 1 >= st && k + 1 < e && q.y < p) +
+                 (k + 2 >= st && k + 2 < e && q.z < p) + (k + 3 < e && q.w < p);
+        }
     } else {                            // sorted by k_sort_big: lower bound of p
         int lo = 0, hi = c;
         while (lo < hi) {

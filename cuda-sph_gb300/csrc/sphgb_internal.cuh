@@ -465,7 +465,8 @@ constexpr int kMinBigVoxel = 16;
 cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
 // tasks (optional): one (voxel, first slot) entry per run of up to 32 sorted
-// slots of a voxel, appended at task_count
+// slots of a voxel, appended at task_count.  tmp_pid must be 16-byte aligned
+// with 4 entries of room past n (the rank count reads it in aligned quads).
 cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* slot,
                                const int32_t* pid, const int32_t* tmp_pid, const int32_t* vstart,
                                const int32_t* vcount, const float4* pos, const float4* vel,
