@@ -659,104 +659,106 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
             float4* __restrict__ force_out, PidRange range, RareList rare) {
+    // kForceRare: a grid-stride loop over the deferred particles; otherwise one
+    // particle per thread (the body runs once)
     const int m_rare = kMode == kForceRare ? *rare.count : 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
-    int s, row = 0;
-    if (kMode == kForceRare) {
-        if (k >= m_rare) return;
-        row = rare.idx[rare.base + k];
-        s = kRange ? __ldg(range.slot_of + row) : row;
-    } else if (kRange) {
-        row = range.i0 + k;
-        if (row >= range.i1) return;
-        s = __ldg(range.slot_of + row);
-    } else {
-        s = k;
-        if (s >= n) return;
-    }
-    const int si = scene_of(s, pbegin, n_scenes);
-    const SceneDev& sc = scenes[si];
-    const float4 pi = __ldg(pos + s);
-    const float4 vi = __ldg(vel + s);
-    float4 fa, fb;
-    ldg256(fin + 2 * s, fa, fb);
-    const float2 ai = make_float2(fa.w, fb.w);
-    const float rho_i = __ldg(rho + s);
-    const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
-    const int32_t* list = nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr;
-    Forces f;
-    if (kMode == kForceLean) {
-        ForceSums<false> fs;
-        bool ok = cnt >= 0 && fabsf(ai.x * ai.y) < INFINITY;
-        if (ok) {
-            force_sums_list<false>(pi, vi, ai.x, sc, fin, list, n, cnt, fs);
-            ok = !fs.bad;
+        int s, row = 0;
+        if (kMode == kForceRare) {
+            if (k >= m_rare) return;
+            row = rare.idx[rare.base + k];
+            s = kRange ? __ldg(range.slot_of + row) : row;
+        } else if (kRange) {
+            row = range.i0 + k;
+            if (row >= range.i1) return;
+            s = __ldg(range.slot_of + row);
+        } else {
+            s = k;
+            if (s >= n) return;
         }
-        if (!ok) {
-            rare.idx[rare.base + atomicAdd(rare.count, 1)] = kRange ? row : s;
-            return;
+        const int si = scene_of(s, pbegin, n_scenes);
+        const SceneDev& sc = scenes[si];
+        const float4 pi = __ldg(pos + s);
+        const float4 vi = __ldg(vel + s);
+        float4 fa, fb;
+        ldg256(fin + 2 * s, fa, fb);
+        const float2 ai = make_float2(fa.w, fb.w);
+        const float rho_i = __ldg(rho + s);
+        const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
+        const int32_t* list = nbr.idx ? nbr.idx + (size_t)s * kListCap : nullptr;
+        Forces f;
+        if (kMode == kForceLean) {
+            ForceSums<false> fs;
+            bool ok = cnt >= 0 && fabsf(ai.x * ai.y) < INFINITY;
+            if (ok) {
+                force_sums_list<false>(pi, vi, ai.x, sc, fin, list, n, cnt, fs);
+                ok = !fs.bad;
+            }
+            if (!ok) {
+                rare.idx[rare.base + atomicAdd(rare.count, 1)] = kRange ? row : s;
+                return;
+            }
+            f = Forces{{fs.px.s, fs.py.s, fs.pz.s}, {fs.vx.s, fs.vy.s, fs.vz.s}, fs.terms};
+        } else {
+            f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, list, n, cnt);
         }
-        f = Forces{{fs.px.s, fs.py.s, fs.pz.s}, {fs.vx.s, fs.vy.s, fs.vz.s}, fs.terms};
-    } else {
-        f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, list, n, cnt);
-    }
-    const float vscale = sc.mass * sc.visc * ai.y;
-    // result_force = ext + -P + V (base_kernels.py:46-52)
-    float F[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) F[a] = (sc.ext[a] + -f.p[a]) + visc_term(f, a, vscale);
-    float v[3] = {vi.x, vi.y, vi.z};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
-    const int p_id = __ldg(pid + s);
-    if (!kPipe || sc.mode == 0) {
-        float x[3] = {pi.x, pi.y, pi.z};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            x[a] = x[a] + v[a] * sc.dt;
-            bool bounced = false;
-            if (x[a] < 0.0f) { x[a] = sc.wall_lo; bounced = true; }
-            if (x[a] > sc.space[a]) { x[a] = sc.wall_hi[a]; bounced = true; }
-            if (bounced) v[a] = -v[a] * sc.damp;
+        const float vscale = sc.mass * sc.visc * ai.y;
+        // result_force = ext + -P + V (base_kernels.py:46-52)
+        float F[3];
+    #pragma unroll
+        for (int a = 0; a < 3; ++a) F[a] = (sc.ext[a] + -f.p[a]) + visc_term(f, a, vscale);
+        float v[3] = {vi.x, vi.y, vi.z};
+    #pragma unroll
+        for (int a = 0; a < 3; ++a) v[a] = v[a] + (F[a] / rho_i) * sc.dt;
+        const int p_id = __ldg(pid + s);
+        if (!kPipe || sc.mode == 0) {
+            float x[3] = {pi.x, pi.y, pi.z};
+    #pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                x[a] = x[a] + v[a] * sc.dt;
+                bool bounced = false;
+                if (x[a] < 0.0f) { x[a] = sc.wall_lo; bounced = true; }
+                if (x[a] > sc.space[a]) { x[a] = sc.wall_hi[a]; bounced = true; }
+                if (bounced) v[a] = -v[a] * sc.damp;
+            }
+            pos_out[s] = make_float4(x[0], x[1], x[2], 0.0f);
+            if (kPipe && pos64_out) {
+                pos64_out[3 * s + 0] = x[0];
+                pos64_out[3 * s + 1] = x[1];
+                pos64_out[3 * s + 2] = x[2];
+            }
+            if (kRange) {
+                range.pos[3 * (size_t)row + 0] = x[0];
+                range.pos[3 * (size_t)row + 1] = x[1];
+                range.pos[3 * (size_t)row + 2] = x[2];
+            }
+        } else if (kPipe) {
+            // pipe flow: FP64 position accumulator and FP64 wall response
+            double x[3], vd[3];
+    #pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                vd[a] = (double)v[a];
+                x[a] = __dadd_rn(pos64[3 * s + a], __dmul_rn(vd[a], sc.dt_d));
+            }
+            PipeView P{pipe + 5 * sc.pipe_off, sc.pipe_rows};
+            pipe_collide(x, vd, P, sc.seed, (uint32_t)p_id, (uint32_t)__ldg(scene_step + si));
+    #pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                v[a] = (float)vd[a];
+                pos64_out[3 * s + a] = x[a];
+                if (kRange) range.pos[3 * (size_t)row + a] = x[a];
+            }
+            pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
         }
-        pos_out[s] = make_float4(x[0], x[1], x[2], 0.0f);
-        if (kPipe && pos64_out) {
-            pos64_out[3 * s + 0] = x[0];
-            pos64_out[3 * s + 1] = x[1];
-            pos64_out[3 * s + 2] = x[2];
-        }
+        vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
         if (kRange) {
-            range.pos[3 * (size_t)row + 0] = x[0];
-            range.pos[3 * (size_t)row + 1] = x[1];
-            range.pos[3 * (size_t)row + 2] = x[2];
+            range.vel[3 * (size_t)row + 0] = v[0];
+            range.vel[3 * (size_t)row + 1] = v[1];
+            range.vel[3 * (size_t)row + 2] = v[2];
         }
-    } else if (kPipe) {
-        // pipe flow: FP64 position accumulator and FP64 wall response
-        double x[3], vd[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            vd[a] = (double)v[a];
-            x[a] = __dadd_rn(pos64[3 * s + a], __dmul_rn(vd[a], sc.dt_d));
-        }
-        PipeView P{pipe + 5 * sc.pipe_off, sc.pipe_rows};
-        pipe_collide(x, vd, P, sc.seed, (uint32_t)p_id, (uint32_t)__ldg(scene_step + si));
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            v[a] = (float)vd[a];
-            pos64_out[3 * s + a] = x[a];
-            if (kRange) range.pos[3 * (size_t)row + a] = x[a];
-        }
-        pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
-    }
-    vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
-    if (kRange) {
-        range.vel[3 * (size_t)row + 0] = v[0];
-        range.vel[3 * (size_t)row + 1] = v[1];
-        range.vel[3 * (size_t)row + 2] = v[2];
-    }
-    pid_out[s] = p_id;
-    if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
-    if (kMode != kForceRare) return;
+        pid_out[s] = p_id;
+        if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
+        if (kMode != kForceRare) return;
     }
 }
 
