@@ -1013,11 +1013,11 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     SPHGB_CUDA(cudaMemsetAsync(ctx->big_count, 0, kCounters * sizeof(int32_t), st));
     {
         const Launch L = ctx->launch(st);
+        // parts start on whole warps (the hash aggregates its atomics per warp)
+        auto bound = [&](int q) {
+            return (int)std::min(N, ((N * q / kHostPosChunks) + 31) & ~(size_t)31);
+        };
         for (int k = 0; k < kHostPosChunks; ++k) {
-            // parts start on whole warps (the hash aggregates its atomics per warp)
-            auto bound = [&](int q) {
-                return (int)std::min(N, ((N * q / kHostPosChunks) + 31) & ~(size_t)31);
-            };
             const int i0 = bound(k);
             const int i1 = k + 1 == kHostPosChunks ? (int)N : bound(k + 1);
             if (i1 <= i0) continue;
