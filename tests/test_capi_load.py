@@ -64,6 +64,10 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lib):
     assert lib.sphgb_ctx_step(None, 1, 0, None) == -1
     with pytest.raises(_capi.SphgbError):
         _capi.call("sphgb_ctx_step", None, 1, 0, None)
+    assert lib.sphgb_compute_next_state_host(None, None, None, None, None, None) == -1
+    assert "ctx is null" in _capi.last_error()
+    assert lib.sphgb_ctx_set_host_order(None, _capi.HOST_ORDER_SLOT) == -1
+    assert "ctx is null" in _capi.last_error()
 
 
 def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):

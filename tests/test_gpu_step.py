@@ -303,3 +303,23 @@ def test_host_entry_page_locked_buffers_match_pageable():
         np.testing.assert_array_equal(op, pageable[0])
         np.testing.assert_array_equal(orho, pageable[2])
         b.close()
+
+
+def test_host_order_rejects_unknown_values():
+    """sphgb_ctx_set_host_order takes AUTO, SLOT or PARTICLE only; a refused
+    value leaves the context usable and its results unchanged."""
+    torch_cuda()
+    from sphgb import _capi
+    from sphgb.device import SceneBatch
+    spec, st = _scenes()["config0"]
+    b = SceneBatch([spec])
+    with pytest.raises(_capi.SphgbError, match="order must be") as e:
+        b.set_host_order(7)
+    assert e.value.code == -1
+    ref_b = SceneBatch([spec])
+    got = b.compute_next_state_host(st.position, st.velocity)
+    want = ref_b.compute_next_state_host(st.position, st.velocity)
+    for a, c in zip(got, want):
+        np.testing.assert_array_equal(a, c)
+    b.close()
+    ref_b.close()
