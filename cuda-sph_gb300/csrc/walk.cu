@@ -678,10 +678,13 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
         }
         const int si = scene_of(s, pbegin, n_scenes);
         const SceneDev& sc = scenes[si];
-        const float4 pi = __ldg(pos + s);
-        const float4 vi = __ldg(vel + s);
+        // the particle's own force record holds its position and velocity too
+        // (written from this state by the density pass, k_gather_vel or
+        // k_force_inputs), so one 32-byte load serves for both
         float4 fa, fb;
         ldg256(fin + 2 * s, fa, fb);
+        const float4 pi = make_float4(fa.x, fa.y, fa.z, 0.0f);
+        const float4 vi = make_float4(fb.x, fb.y, fb.z, 0.0f);
         const float2 ai = make_float2(fa.w, fb.w);
         const float rho_i = __ldg(rho + s);
         const int cnt = nbr.count ? __ldg(nbr.count + s) : -1;
