@@ -76,7 +76,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["config2", "box2m", "config0"], default="config2")
+    ap.add_argument("--workload", choices=["config2", "box2m", "config0", "config1"],
+                    default="config2")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-steps", type=int, default=10, help="oracle steps of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -96,7 +97,8 @@ def parse_args():
 
 METRIC = {"config2": "particle-steps/s (4M box, 1 GB300)",
           "box2m": "particle-steps/s (2M box, 1 GB300)",
-          "config0": "particle-steps/s (8k box, 1 GB300)"}
+          "config0": "particle-steps/s (8k box, 1 GB300)",
+          "config1": "particle-steps/s (262k pipe start state, 1 GB300)"}
 
 
 def workload(name):
@@ -112,6 +114,12 @@ def workload(name):
         spec, st = scenes.box_dam_break(nx=100, ny=200, nz=100, spacing=0.005, jitter=0.0005,
                                         box=(2.0, 2.0, 2.0), h=0.0112, mass=1.25e-4, seed=2)
         desc = "2M-particle dam-break box (100x200x100 lattice, spacing 0.005, h 0.0112, [0,2]^3)"
+    elif name == "config1":
+        # the pipe flow's start state: ~133 particles per voxel, so the density
+        # pass takes its dense-walk path (a profiling and parity case)
+        spec, st = scenes.config1()
+        desc = ("262k-particle pipe flow start state (3-segment pipe, radii 0.10/0.06/0.10, "
+                "h 0.02, ~133 particles per voxel)")
     else:
         spec, st = scenes.config0()
         desc = "8k-particle dam-break box (16x32x16 lattice, h 0.045), 32-neighbour cap"
@@ -210,12 +218,13 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def committed_traffic(stage):
+def committed_traffic(stage, workload="config2"):
     """DRAM bytes per launch of a stage's kernel from the committed ncu summary
-    (profiles/<kernel>_config2.md, line 'traffic_bytes_per_launch: X')."""
+    of this workload (profiles/<kernel>_<workload>.md, line
+    'traffic_bytes_per_launch: X'), or None when there is none."""
     names = {"force_integrate": "k_integrate", "density": "k_density_wc",
              "rank_gather": "k_rank_gather"}
-    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_config2.md")
+    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_{workload}.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -225,34 +234,53 @@ def committed_traffic(stage):
     return None
 
 
-def cpu_baseline(spec, state, steps):
+def cpu_baseline(spec, state, steps, step_index=0):
     from oracle import ref
     import numpy as np
     sp = ref.params_from_spec(spec)
     pos = np.ascontiguousarray(state.position, dtype=np.float64)
     vel = np.ascontiguousarray(state.velocity, dtype=np.float64)
+    pipe = spec.params.pipe.to_numpy() if spec.mode == 'PIPE' else None
     # like the timed GPU steps: every step is a full step of the step-0 state
     t0 = time.perf_counter()
     for _ in range(steps):
-        out = ref.step(sp, pos, vel, step_index=0)
+        out = ref.step(sp, pos, vel, pipe=pipe, step_index=step_index)
     dt = time.perf_counter() - t0
     return {"value": spec.n * steps / dt, "unit": "particle-steps/s", "cores": ref.num_threads(),
             "kind": "port", "sample": f"{steps} full steps of the {spec.n}-particle scene's step-0 "
                                      f"state ({dt:.1f} s wall, FP64 C/OpenMP restatement)"}, out
 
 
-def oracle_error(got, want):
+def oracle_error(got, want, pos_in=None, dt=None):
     """The GPU step against the FP64 oracle's step of the same input: density
     relative error, position absolute error, and velocity error over the
     largest velocity (cancellation in the force sum makes a per-particle
-    relative velocity error meaningless)."""
+    relative velocity error meaningless).  For a pipe scene (pos_in and dt
+    given), particles whose wall response or respawn fired on either side are
+    counted apart: at the wall, an FP32 and an FP64 velocity can land on
+    different sides of a decision, so those particles are reported on their own."""
     import numpy as np
     (gp, gv, gr), (wp, wv, wr) = got, want
     ok = np.isfinite(wr) & (wr > 0)
-    return {"density_max_rel": float(np.max(np.abs(gr[ok] - wr[ok]) / wr[ok])),
-            "position_max_abs": float(np.max(np.abs(gp - wp))),
-            "velocity_max_abs_over_max": float(np.max(np.abs(gv - wv)) / np.max(np.abs(wv))),
-            "particles_compared": int(ok.sum())}
+    out = {"density_max_rel": float(np.max(np.abs(gr[ok] - wr[ok]) / wr[ok])),
+           "particles_compared": int(ok.sum())}
+    free = np.ones(len(gp), dtype=bool)
+    if pos_in is not None:
+        with np.errstate(invalid="ignore"):
+            def fired(v, x):
+                return ~np.all(np.abs(pos_in + v * dt - x) <= 1e-9 * np.maximum(np.abs(x), 1.0), axis=1)
+            wall = fired(wv, wp) | fired(gv, gp)
+        free = ~wall
+        out["wall_response_particles"] = int(wall.sum())
+        if wall.any():
+            dw = np.abs(gp[wall] - wp[wall])
+            out["wall_position_max_abs"] = float(np.max(dw))
+            # the parity tests' bound for these particles: 1e-3 of |x|
+            out["wall_within_1e-3"] = int(np.all(dw <= 1e-3 * np.maximum(np.abs(wp[wall]), 1.0),
+                                                 axis=1).sum())
+    out["position_max_abs"] = float(np.max(np.abs(gp[free] - wp[free])))
+    out["velocity_max_abs_over_max"] = float(np.max(np.abs(gv[free] - wv[free])) / np.max(np.abs(wv)))
+    return out
 
 
 def run_gb300(args):
@@ -315,12 +343,18 @@ def run_gb300(args):
     step_bytes = (192 * n + 12 * batch.n_voxels)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": committed_traffic(dom), "algorithmic_bytes": b_alg,
+                "traffic": committed_traffic(dom, args.workload), "algorithmic_bytes": b_alg,
                 "kernel_ms": round(stages[dom], 4)}
     step_roofline = {"algorithmic_bytes_per_step": step_bytes,
                      "achieved": round(step_bytes / (ms / args.steps / 1e3) / 1e9, 1),
                      "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
                      "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
+
+    # per-step working set: state and sort buffers (~100 B), neighbour list
+    # (128 B) and force inputs (32 B) per particle, 12 B per voxel
+    ws = 260 * n + 12 * batch.n_voxels
+    l2_note = (f"inputs larger than L2 (~{ws / 1e9:.2f} GB per step > 129 MB)" if ws > 129e6 else
+               f"working set ~{ws / 1e6:.0f} MB fits in the 129 MB L2")
 
     # free-running simulation from the same start (informational): the
     # reference's formulas make this scene blow up within a few steps
@@ -354,6 +388,8 @@ def run_gb300(args):
         batch.compute_next_state_host(h_pos, h_vel, o_pos, o_vel, o_rho)
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world, dev)
+    # the scene's step counter of the last call (keys a pipe's respawn draws)
+    e2e_step = int(batch.steps[0].item()) - 1
     log(f"e2e {k_e2e} steps: {e2e_s:.3f} s")
     e2e = {"value": n * k_e2e * world / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 56 * n, "steps": k_e2e,
@@ -365,7 +401,7 @@ def run_gb300(args):
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": desc, "particles": n, "voxels": batch.n_voxels,
-                      "l2": "inputs larger than L2 (state + sort buffers ~0.4 GB > 129 MB)",
+                      "l2": l2_note,
                       "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step",
                       "input": "every step is a full step of the same resident step-0 state"},
            "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
@@ -375,10 +411,16 @@ def run_gb300(args):
                         "ms_per_step": summary(tried)},
            "clocks": clocks, "gpu_launches": kernels_per_step(batch.n_voxels) * args.steps}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"], want = cpu_baseline(spec, state, max(args.cpu_steps, 1))
+        out["cpu_baseline"], want = cpu_baseline(spec, state, max(args.cpu_steps, 1),
+                                                 step_index=e2e_step)
         log(f"cpu baseline: {out['cpu_baseline']}")
-        # the end-to-end outputs are one step of the same step-0 state
-        out["oracle_err"] = oracle_error((o_pos, o_vel, o_rho), want)
+        # the end-to-end outputs are one step of the same step-0 state, at the
+        # step index of the last call
+        pipe_scene = spec.mode == 'PIPE'
+        out["oracle_err"] = oracle_error(
+            (o_pos, o_vel, o_rho), want,
+            pos_in=np.asarray(state.position, dtype=np.float64) if pipe_scene else None,
+            dt=float(np.float32(1.0 / spec.params.fps)) if pipe_scene else None)
         log(f"error against the FP64 oracle: {out['oracle_err']}")
     batch.close()
     if not args.no_batched and args.workload == "config2":
@@ -507,14 +549,15 @@ def run_reference(args):
     from oracle import ref
     spec, state, desc = workload(args.workload)
     sp = ref.params_from_spec(spec)
+    pipe = spec.params.pipe.to_numpy() if spec.mode == 'PIPE' else None
     pos = np.ascontiguousarray(state.position, dtype=np.float64)
     vel = np.ascontiguousarray(state.velocity, dtype=np.float64)
     # like the GPU arm, every step is a full step of the same step-0 state
     for _ in range(max(args.warmup, 0)):
-        ref.step(sp, pos, vel, step_index=0)
+        ref.step(sp, pos, vel, pipe=pipe, step_index=0)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ref.step(sp, pos, vel, step_index=0)
+        ref.step(sp, pos, vel, pipe=pipe, step_index=0)
     dt = time.perf_counter() - t0
     value = spec.n * args.steps / dt
     cores = ref.num_threads()

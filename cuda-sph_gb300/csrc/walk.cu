@@ -649,7 +649,7 @@ constexpr int kRareBlocks = 152;   // kForceRare grid (one block per SM)
 // arithmetic), which also writes the FP64 rows of the next position and
 // velocity.  kMode: see kForceAll.
 template <bool kPipe, bool kRange, int kMode>
-__global__ void __launch_bounds__(kBlock, kPipe ? 1 : 4)
+__global__ void __launch_bounds__(kBlock, 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
             const float4* __restrict__ vel, const float* __restrict__ rho,
