@@ -218,6 +218,21 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def committed_inst_per_particle(stage, workload="config2"):
+    """Warp instructions per particle of a stage's kernel from the committed ncu
+    summary of this workload (its '... N warp instructions per particle.'
+    line), or None when there is none."""
+    import re
+    names = {"force_integrate": "k_integrate", "density": "k_density_wc",
+             "rank_gather": "k_rank_gather"}
+    p = os.path.join(ROOT, "profiles", f"{names.get(stage, stage)}_{workload}.md")
+    try:
+        m = re.search(r"(\d+) warp instructions per particle", open(p).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
 def committed_traffic(stage, workload="config2"):
     """DRAM bytes per launch of a stage's kernel from the committed ncu summary
     of this workload (profiles/<kernel>_<workload>.md, line
@@ -350,6 +365,19 @@ def run_gb300(args):
                      "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
                      "stage_ms": {k: round(v, 4) for k, v in stages.items()}}
 
+    # The dominant kernel is bound by instruction issue, not DRAM: its warp
+    # instructions (per particle, from the committed ncu summary) over its
+    # live time, against one warp instruction per cycle on each of the 152 x 4
+    # SM sub-partitions at the SM clock sampled during the timed region.
+    ipp = committed_inst_per_particle(dom, args.workload)
+    issue_roofline = None
+    if ipp and clocks.get("sm_mhz"):
+        got = ipp * n / (stages[dom] / 1e3)
+        top = 152 * 4 * clocks["sm_mhz"] * 1e6
+        issue_roofline = {"kernel": dom, "warp_instructions_per_particle": ipp,
+                          "achieved": round(got / 1e12, 4), "peak": round(top / 1e12, 4),
+                          "unit": "1e12 warp instructions/s", "frac": round(got / top, 4)}
+
     # per-step working set: state and sort buffers (~100 B), neighbour list
     # (128 B) and force inputs (32 B) per particle, 12 B per voxel
     ws = 260 * n + 12 * batch.n_voxels
@@ -404,7 +432,8 @@ def run_gb300(args):
                       "l2": l2_note,
                       "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step",
                       "input": "every step is a full step of the same resident step-0 state"},
-           "e2e": e2e, "roofline": roofline, "step_roofline": step_roofline,
+           "e2e": e2e, "roofline": roofline, "issue_roofline": issue_roofline,
+           "step_roofline": step_roofline,
            "free_running": free,
            "autotune": {"chosen": {"density": {0: "warp", 1: "thread"}[best.density_variant],
                                    "sort_block": best.sort_block, "big_voxel": best.big_voxel},
