@@ -2,7 +2,8 @@
 
 Each translation unit under ``csrc/`` is compiled by its own nvcc process, in
 parallel, then linked into ``sphgb/libsphgb.so``.  The CUDA runtime is linked
-statically, so the library only needs the driver at run time.  No fast-math:
+statically, so the library only needs the NVIDIA kernel driver (libcuda) at
+run time.  No fast-math:
 the kernels rely on IEEE division, square root and denormals for the exact
 voxel and neighbour decisions.
 """
