@@ -249,6 +249,53 @@ def committed_traffic(stage, workload="config2"):
     return None
 
 
+def profile_source(stage, workload="config2"):
+    """Where the committed per-kernel figures (DRAM traffic, warp
+    instructions) come from: the ncu summary file and the case it captured,
+    read from its 'case:' line.  These figures are not measured in this run."""
+    names = {"force_integrate": "k_integrate", "density": "k_density_wc",
+             "rank_gather": "k_rank_gather"}
+    rel = os.path.join("profiles", f"{names.get(stage, stage)}_{workload}.md")
+    case = None
+    try:
+        for line in open(os.path.join(ROOT, rel)):
+            if line.startswith("case:"):
+                case = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        return None
+    return {"file": rel, "case": case, "measured_in_this_run": False}
+
+
+def scene_facts(batch):
+    """Facts of a batch's current state: non-finite particles, mean capped
+    and uncapped neighbour counts (self included, the reference's
+    get_neighbours counts) and the FP64 conservation sums per scene."""
+    import numpy as np
+    pos, vel, _ = batch.export_aos_f64()
+    nonfinite = int((~(pos.isfinite().all(dim=1) & vel.isfinite().all(dim=1))).sum())
+    cons = batch.conservation()
+    cap, unc = batch.neighbour_counts()
+    return {"nonfinite_particles": nonfinite,
+            "neighbours_capped_mean": round(float(np.mean(cap)), 3) if len(cap) else 0.0,
+            "neighbours_uncapped_mean": round(float(np.mean(unc)), 3) if len(unc) else 0.0}, cons
+
+
+def drift(cons0, cons1):
+    """Conservation drift between two FP64 conservation records (S, 8):
+    total mass change (relative), total momentum change (relative to the
+    summed |momentum| scale) and total energy change (relative to |E0|)."""
+    import numpy as np
+    c0, c1 = np.asarray(cons0).sum(0), np.asarray(cons1).sum(0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        p0, p1 = c0[1:4], c1[1:4]
+        return {"mass_rel": float(abs(c1[0] - c0[0]) / c0[0]) if c0[0] else 0.0,
+                "momentum_change": [float(x) for x in (p1 - p0)],
+                "kinetic_start": float(c0[4]), "kinetic_end": float(c1[4]),
+                "energy_start": float(c0[6]), "energy_end": float(c1[6]),
+                "energy_rel": float(abs(c1[6] - c0[6]) / abs(c0[6])) if c0[6] else None}
+
+
 def cpu_baseline(spec, state, steps, step_index=0):
     from oracle import ref
     import numpy as np
@@ -304,6 +351,7 @@ def run_gb300(args):
     rank, world, local = dist_setup(args, "nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     from sphgb.device import SceneBatch
     spec, state, desc = workload(args.workload)
     n = spec.n
@@ -358,8 +406,10 @@ def run_gb300(args):
     step_bytes = (192 * n + 12 * batch.n_voxels)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                 "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": committed_traffic(dom, args.workload), "algorithmic_bytes": b_alg,
-                "kernel_ms": round(stages[dom], 4)}
+                "traffic": committed_traffic(dom, args.workload),
+                "traffic_source": profile_source(dom, args.workload),
+                "algorithmic_bytes": b_alg, "kernel_ms": round(stages[dom], 4),
+                "kernel_ms_source": "CUDA events around the kernel in this run"}
     step_roofline = {"algorithmic_bytes_per_step": step_bytes,
                      "achieved": round(step_bytes / (ms / args.steps / 1e3) / 1e9, 1),
                      "frac": round(step_bytes / (ms / args.steps / 1e3) / 1e9 / peak, 4),
@@ -367,14 +417,15 @@ def run_gb300(args):
 
     # The dominant kernel is bound by instruction issue, not DRAM: its warp
     # instructions (per particle, from the committed ncu summary) over its
-    # live time, against one warp instruction per cycle on each of the 152 x 4
-    # SM sub-partitions at the SM clock sampled during the timed region.
+    # live time, against one warp instruction per cycle on each of the SMs' 4
+    # sub-partitions at the SM clock sampled during the timed region.
     ipp = committed_inst_per_particle(dom, args.workload)
     issue_roofline = None
     if ipp and clocks.get("sm_mhz"):
         got = ipp * n / (stages[dom] / 1e3)
-        top = 152 * 4 * clocks["sm_mhz"] * 1e6
+        top = sms * 4 * clocks["sm_mhz"] * 1e6
         issue_roofline = {"kernel": dom, "warp_instructions_per_particle": ipp,
+                          "warp_instructions_source": profile_source(dom, args.workload),
                           "achieved": round(got / 1e12, 4), "peak": round(top / 1e12, 4),
                           "unit": "1e12 warp instructions/s", "frac": round(got / top, 4)}
 
@@ -388,14 +439,16 @@ def run_gb300(args):
     # reference's formulas make this scene blow up within a few steps
     batch.bind_output(False)
     k_free = min(args.steps, 10)
+    cons0 = batch.conservation()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     batch.step(k_free, use_graph=False)
     f1.record(stream)
     torch.cuda.synchronize()
-    free = {"steps": k_free, "ms_per_step": f0.elapsed_time(f1) / k_free,
-            "nonfinite_particles": int((~torch.isfinite(batch.pos[:, :3]).all(dim=1)).sum())}
+    facts, cons1 = scene_facts(batch)
+    free = {"steps": k_free, "ms_per_step": f0.elapsed_time(f1) / k_free, **facts,
+            "conservation_drift": drift(cons0, cons1)}
     log(f"free running: {free}")
 
     # end to end through the C ABI host-buffer entry point: each step copies
@@ -429,7 +482,7 @@ def run_gb300(args):
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": desc, "particles": n, "voxels": batch.n_voxels,
-                      "l2": l2_note,
+                      "l2": l2_note, "sms": sms,
                       "parallelism": f"replicas x{world}", "graph": "one CUDA graph per step",
                       "input": "every step is a full step of the same resident step-0 state"},
            "e2e": e2e, "roofline": roofline, "issue_roofline": issue_roofline,
@@ -487,11 +540,20 @@ def batched_section(args):
     for (spec, st), got in zip(pairs[:8], one):
         _, _, rho = ref.step(ref.params_from_spec(spec), st.position, st.velocity)
         err = max(err, float(np.max(np.abs(got.density - rho) / rho)))
+    # what the workload's state is at its end: the same run again, untimed
+    from sphgb.device import SceneBatch
+    b = SceneBatch([p[0] for p in pairs])
+    b.load_states([p[1] for p in pairs])
+    cons0 = b.conservation()
+    b.step(steps, use_graph=True)
+    facts, cons1 = scene_facts(b)
+    b.close()
     return {"scenes": len(pairs), "particles": sum(p[0].n for p in pairs), "steps": steps,
             "value": work / tb, "unit": "particle-steps/s",
             "plain_value": work / tp, "plain_graph_value": work / tg,
             "vs_plain": tb and tp / tb, "vs_plain_graph": tg / tb,
             "identical_to_plain": bool(same), "density_rel_err_vs_fp64": err,
+            "at_end": facts, "conservation_drift": drift(cons0, cons1),
             "graph": "all scenes and steps in one CUDA graph launch"}
 
 
@@ -508,6 +570,7 @@ def pipe_section(args):
     b.load_states([st])
     b.step(10, use_graph=True)      # captures the 10-step graph
     b.load_states([st])             # back to the start state and step 0
+    start_facts, cons0 = scene_facts(b)
     torch.cuda.synchronize()
     steps = 1000
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -517,13 +580,16 @@ def pipe_section(args):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    nonfinite = int((~torch.isfinite(b.pos[:, :3]).all(dim=1)).sum())
-    cons = b.conservation()[0]
+    facts, cons1 = scene_facts(b)
     b.close()
     log(f"pipe flow: {spec.n} particles x {steps} steps in {ms:.1f} ms")
     return {"particles": spec.n, "steps": steps, "value": spec.n * steps / (ms / 1e3),
             "unit": "particle-steps/s", "ms_per_step": ms / steps,
-            "nonfinite_particles": nonfinite, "mass_fp64": float(cons[0]),
+            "at_start": start_facts, "at_end": facts,
+            "mass_fp64": float(cons1[0][0]), "conservation_drift": drift(cons0, cons1),
+            "note": ("under the reference's formulas this flow collapses into dense clusters "
+                     "(the at_start/at_end neighbour counts): the rate is that of ~thousands of "
+                     "candidates within h per particle, not of the start state"),
             "graph": "10 steps per CUDA graph launch"}
 
 
@@ -554,8 +620,11 @@ def served_section(args):
     log(f"served one at a time: {plain_s:.3f} s of GPU time for {work} particle-steps")
     rates = sorted({float(x) for x in args.served_rates.split(",")} | {args.served_rate})
     sweep = []
+    head_reqs = []
     for rate in rates:
         reqs = [dataclasses.replace(r, arrival=r.arrival / rate) for r in base]
+        if rate == args.served_rate:
+            head_reqs = reqs
         server = SceneServer(hbm_budget_bytes=150e9, max_tick_steps=64)
         st = server.run(reqs)
         server.close()
@@ -566,8 +635,50 @@ def served_section(args):
                       "max_active": st.max_active, "ticks": st.ticks, "repacks": st.repacks,
                       "vs_plain": st.throughput / (work / plain_s)})
     head = next(s for s in sweep if s["rate_per_s"] == args.served_rate)
+    # What the GPU gives for this mix with every request resident at once: one
+    # batch of all requests' start states, 100 steps in one graph launch.  No
+    # schedule can serve the mix faster than this (it has no arrivals, no
+    # retirements and every request at its largest overlap), so it bounds the
+    # served rate, and bound / plain bounds the served speed-up.
+    import numpy as np
+    from oracle import ref
+    b = SceneBatch([r.spec for r in base])
+    b.load_states([r.state for r in base])
+    b.step(100, use_graph=True)              # captures the graph
+    b.load_states([r.state for r in base])
+    start_facts, _ = scene_facts(b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.step(100, use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    mix_rate = b.n * 100 / (e0.elapsed_time(e1) / 1e3)
+    # density error of the mix's first step against the FP64 oracle, the first
+    # 8 requests (box and pipe scenes as they come)
+    b.load_states([r.state for r in base])
+    b.step(1)
+    got = b.states()
+    b.close()
+    err = 0.0
+    for r, g in zip(base[:8], got[:8]):
+        pipe = r.spec.params.pipe.to_numpy() if r.spec.mode == 'PIPE' else None
+        _, _, rho = ref.step(ref.params_from_spec(r.spec), r.state.position, r.state.velocity,
+                             pipe=pipe)
+        ok = rho > 0
+        err = max(err, float(np.max(np.abs(g.density[ok] - rho[ok]) / rho[ok])))
+    nonfinite = sum(int((~np.isfinite(r.result.position).all(1)).sum())
+                    for r in head_reqs if r.result is not None)
+    bound = {"value": mix_rate, "unit": "particle-steps/s", "steps": 100,
+             "particles": sum(r.spec.n for r in base),
+             "vs_plain": mix_rate / (work / plain_s), "at_start": start_facts,
+             "how": "all requests resident in one batch, 100 steps in one graph launch"}
     return {"requests": len(base), "particle_steps": work, "unit": "particle-steps/s",
-            "plain_value": work / plain_s, "hbm_budget_gb": 150, **head, "sweep": sweep}
+            "plain_value": work / plain_s, "hbm_budget_gb": 150, **head, "sweep": sweep,
+            "mix_bound": bound, "density_rel_err_vs_fp64": err,
+            "box_requests": sum(r.spec.mode == 'BOX' for r in base),
+            "pipe_requests": sum(r.spec.mode == 'PIPE' for r in base),
+            "nonfinite_particles_in_results": nonfinite}
 
 
 def run_reference(args):

@@ -9,6 +9,7 @@
 // abstract_sph_strategy.py:31-46, voxel_sph_strategy.py:20-116) without any
 // host round trip.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -25,6 +26,27 @@
 #include "../../include/sphgb.h"
 
 using namespace sphgb;
+
+int sphgb::device_sm_count() {
+    constexpr int kCached = 64;
+    static std::atomic<int> cache[kCached] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev >= 0 && dev < kCached) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev >= 0 && dev < kCached) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
 
 namespace {
 
@@ -109,6 +131,13 @@ struct SphgbCtx {
                                       // [3 + r] deferred particles of force pass r (kCounters)
     int32_t* rare = nullptr;          // deferred particles of the force pass (RareList)
     int2* tasks = nullptr;             // (voxel, first slot) per run of <= 32 slots
+    // the neighbour rows in nbr, pidB and posB are those of the latest step
+    // (cleared by anything else that sorts into the B buffers)
+    bool nbr_valid = false;
+    // checked mode (sphgb_ctx_set_checks): a validation kernel after every
+    // step ORs SPHGB_CHECK_* bits into d_check[0] (see k_check_step)
+    bool checks = false;
+    uint32_t* d_check = nullptr;
     // bound (caller-owned) state
     float4* posA = nullptr;
     float4* velA = nullptr;
@@ -192,7 +221,8 @@ void free_ctx(SphgbCtx* c) {
     void* ptrs[] = {c->d_scenes, c->d_scenes_ref, c->d_pbegin, c->d_pipe, c->cell, c->slot_of, c->slot, c->tmp_pid,
                     c->vstart, c->vcount, c->tile_sums, c->posB, c->velB, c->pidB,
                     c->pos64B, c->fin, c->owned, c->stage, c->d_chunks, c->d_partials,
-                    c->big_list, c->big_count, c->rare, c->nbr.idx, c->nbr.count, c->tasks};
+                    c->big_list, c->big_count, c->rare, c->nbr.idx, c->nbr.count, c->tasks,
+                    c->d_check};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
@@ -378,6 +408,101 @@ __global__ void k_by_pid(const int32_t* __restrict__ pbegin, int n_scenes, int n
     if (b_out) b_out[i] = b[s];
 }
 
+// The step's neighbour rows (slots of the sorted state) -> rows in original
+// particle order holding scene-local particle ids, -1 padded.
+__global__ void k_export_neighbours(const int32_t* __restrict__ pbegin, int n_scenes, int n,
+                                    const int32_t* __restrict__ pid, NbrList nbr,
+                                    int32_t* __restrict__ list_out, int32_t* __restrict__ count_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = __ldg(pbegin + scene_of(s, pbegin, n_scenes)) + pid[s];
+    const int c = nbr.count[s];
+    if (count_out) count_out[i] = c;
+    if (!list_out) return;
+    const int32_t* row = nbr.idx + (size_t)s * kListCap;
+    int32_t* out = list_out + (size_t)i * kListCap;
+    for (int k = 0; k < kListCap; ++k) out[k] = k < c ? pid[row[k]] : -1;
+}
+
+// Checked mode: one thread per sorted slot of the step's input validates what
+// the step read and wrote, ORs SPHGB_CHECK_* bits into word[0], keeps the
+// smallest original index of a flagged particle in word[1] and counts the
+// flagged particles in word[2].  It only compares indices against their
+// ranges before it uses them, so bad data raises bits, never a fault.  These
+// are the places where the reference has undefined behaviour: voxel ids of
+// particles outside the box (voxel_kernels.py:10-17, :89-105), never-written
+// walk voxels and reads past voxel_begin (:44, :64-65, :70), and non-finite
+// coordinates, which its sort and walk do not expect.
+__global__ void k_check_step(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
+                             int n_scenes, int n, const float4* __restrict__ pos,
+                             const float4* __restrict__ vel, const int32_t* __restrict__ pid,
+                             const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+                             NbrList nbr, const float* __restrict__ rho,
+                             const float4* __restrict__ pos_out, const float4* __restrict__ vel_out,
+                             uint32_t* __restrict__ word) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int si = scene_of(s, pbegin, n_scenes);
+    const SceneDev& sc = scenes[si];
+    const float4 p = pos[s];
+    uint32_t bits = 0;
+    if (!finite3(p) || !finite3(vel[s])) bits |= SPHGB_CHECK_NONFINITE_INPUT;
+    const float xs[3] = {p.x, p.y, p.z};
+    for (int a = 0; a < 3; ++a)
+        if (isfinite(xs[a]) && !(xs[a] >= 0.0f && xs[a] < sc.space[a])) bits |= SPHGB_CHECK_OUT_OF_DOMAIN;
+    // the slot lies inside its own voxel's range, ids ascending within it
+    int vid;
+    if (finite3(p)) {
+        const int vx = voxel_coord(p.x, sc.vs[0], sc.dims[0]);
+        const int vy = voxel_coord(p.y, sc.vs[1], sc.dims[1]);
+        const int vz = voxel_coord(p.z, sc.vs[2], sc.dims[2]);
+        vid = sc.v_begin + voxel_index(vx, vy, vz, sc.tiled, sc.dims[0], sc.dims[1], sc.nt0, sc.nt1);
+    } else {
+        vid = sc.v_begin + sc.v_count;
+    }
+    const int st = vstart[vid], c = vcount[vid];
+    const int p_lo = sc.p_begin, p_hi = sc.p_begin + sc.p_count;
+    if (c <= 0 || st < p_lo || st + c > p_hi || s < st || s >= st + c)
+        bits |= SPHGB_CHECK_VOXEL_TABLE;
+    else if (vid != sc.v_begin + sc.v_count && s > st && !(pid[s - 1] < pid[s]))
+        bits |= SPHGB_CHECK_VOXEL_TABLE;
+    const int myid = pid[s];
+    if (myid < 0 || myid >= sc.p_count) bits |= SPHGB_CHECK_VOXEL_TABLE;
+    // neighbour row: other particles of the same scene within h (guard band).
+    // A row holds at most cap others: cap - 1 when the particle itself is
+    // among the first cap accepted, cap when more than cap - 1 neighbours come
+    // before it in walk order.
+    if (nbr.count) {
+        const int cnt = nbr.count[s];
+        if (cnt < -1 || cnt > kListCap || (sc.cap <= kListCap && cnt > sc.cap)) {
+            bits |= SPHGB_CHECK_NEIGHBOUR_LIST;
+        } else {
+            const int32_t* row = nbr.idx + (size_t)s * kListCap;
+            for (int k = 0; k < cnt; ++k) {
+                const int j = row[k];
+                if (j < p_lo || j >= p_hi || j == s) {
+                    bits |= SPHGB_CHECK_NEIGHBOUR_LIST;
+                    break;
+                }
+                const float4 q = pos[j];
+                const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                if (!(dx * dx + dy * dy + dz * dz <= sc.h2_hi * 1.0001f)) {
+                    bits |= SPHGB_CHECK_NEIGHBOUR_LIST;
+                    break;
+                }
+            }
+        }
+    }
+    if (!isfinite(rho[s]) || !finite3(pos_out[s]) || !finite3(vel_out[s]))
+        bits |= SPHGB_CHECK_NONFINITE_OUTPUT;
+    if (bits) {
+        atomicOr(word, bits);
+        const int i = __ldg(pbegin + si) + (myid >= 0 && myid < sc.p_count ? myid : 0);
+        atomicMin(word + 1, (uint32_t)i);
+        atomicAdd(word + 2, 1u);
+    }
+}
+
 // FP64 conservation sums, one block per chunk of one scene, fixed order.
 __global__ void __launch_bounds__(kConsThreads)
 k_cons_partial(const SceneDev* __restrict__ scenes, const ConsChunk* __restrict__ chunks,
@@ -545,6 +670,19 @@ int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range, int rang
     return SPHGB_OK;
 }
 
+// checked mode: validate the step just enqueued (inputs in the B buffers,
+// outputs where enqueue_forces wrote them)
+int enqueue_checks(SphgbCtx* c, cudaStream_t st) {
+    if (!c->checks || c->n == 0) return SPHGB_OK;
+    const bool sep = c->out_pos != nullptr;
+    k_check_step<<<blocks(c->n), kBlock, 0, st>>>(c->d_scenes, c->d_pbegin, c->n_scenes, c->n,
+                                                  c->posB, c->velB, c->pidB, c->vstart, c->vcount,
+                                                  c->nbr, c->rho, sep ? c->out_pos : c->posA,
+                                                  sep ? c->out_vel : c->velA, c->d_check);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
 // enqueue one full step on stream st; ev (optional, 8 events): ev[0] at the
 // start and ev[k] after stage k (see SPHGB_PROFILE_STAGES).  vel_ready
 // (optional): the state in A is in original particle order and its
@@ -582,8 +720,11 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
         SPHGB_CUDA(cudaStreamWaitEvent(st, vel_ready, 0));
         SPHGB_CUDA(launch_gather_vel(L, c->pidB, c->velA, c->rho, c->velB, c->fin));
     }
+    c->nbr_valid = true;
     if (!with_forces) return SPHGB_OK;
     rc = enqueue_forces(c, L, nullptr, 0);
+    if (rc) return rc;
+    rc = enqueue_checks(c, st);
     if (rc) return rc;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[6], st));
     k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
@@ -698,6 +839,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     c->any_pipe = any_pipe;
     // the caller binds (new) state and outputs for the new layout
     c->bound = false;
+    c->nbr_valid = false;
     c->posA = c->velA = nullptr;
     c->rho = nullptr;
     c->pidA = nullptr;
@@ -1093,6 +1235,8 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
             SPHGB_CUDA(cudaMemcpyAsync(h_pos_out + off, sp + off, len, cudaMemcpyDeviceToHost, st2));
             SPHGB_CUDA(cudaMemcpyAsync(h_vel_out + off, sv + off, len, cudaMemcpyDeviceToHost, st2));
         }
+        rc = enqueue_checks(ctx, st);
+        if (rc) return rc;
         k_step_counter<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->scene_step, ctx->n_scenes);
         SPHGB_CUDA(cudaGetLastError());
         SPHGB_CUDA(cudaEventRecord(e_done, st2));
@@ -1143,6 +1287,7 @@ int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_unca
                               ctx->any_pipe ? ctx->pos64A : nullptr, ctx->posB, ctx->velB,
                               ctx->pidB, ctx->any_pipe ? ctx->pos64B : nullptr, ctx->vstart,
                               ctx->vcount);
+    ctx->nbr_valid = false;
     if (rc) return rc;
     // per sorted slot into the scratch id buffers, then to original order
     SPHGB_CUDA(launch_neighbours(L, ctx->posB, ctx->vstart, ctx->vcount, nullptr, 0, ctx->cell,
@@ -1150,6 +1295,60 @@ int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_unca
     k_by_pid<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n, ctx->pidB,
                                                 ctx->cell, ctx->slot, d_capped, d_uncapped);
     SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_step_neighbours(SphgbCtx* ctx, int32_t* d_list, int32_t* d_count, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!d_list && !d_count) return fail(SPHGB_ERR_INVALID, "d_list and d_count are both null");
+    if (!ctx->nbr_valid)
+        return fail(SPHGB_ERR_STATE, "no step has run since the context was configured or re-sorted");
+    if (ctx->n == 0) return SPHGB_OK;
+    cudaStream_t st = as_stream(stream);
+    k_export_neighbours<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                                           ctx->pidB, ctx->nbr, d_list, d_count);
+    SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_set_checks(SphgbCtx* ctx, int enable) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    const bool on = enable != 0;
+    if (on && !ctx->d_check) {
+        int rc = dalloc(&ctx->d_check, 3);
+        if (rc) return rc;
+        const uint32_t init[3] = {0u, 0xffffffffu, 0u};
+        SPHGB_CUDA(cudaMemcpy(ctx->d_check, init, sizeof(init), cudaMemcpyHostToDevice));
+    }
+    if (on != ctx->checks) {
+        // captured step graphs hold the old sequence
+        for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+        ctx->graphs.clear();
+    }
+    ctx->checks = on;
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_check_word(SphgbCtx* ctx, uint32_t* h_word, int clear, void* stream) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (!h_word) return fail(SPHGB_ERR_INVALID, "h_word is null");
+    if (!ctx->d_check) {
+        h_word[0] = 0u;
+        h_word[1] = 0xffffffffu;
+        h_word[2] = 0u;
+        return SPHGB_OK;
+    }
+    cudaStream_t st = as_stream(stream);
+    uint32_t w[3];
+    SPHGB_CUDA(cudaMemcpyAsync(w, ctx->d_check, sizeof(w), cudaMemcpyDeviceToHost, st));
+    SPHGB_CUDA(cudaStreamSynchronize(st));
+    h_word[0] = w[0];
+    h_word[1] = w[1];
+    h_word[2] = w[2];
+    if (clear) {
+        const uint32_t init[3] = {0u, 0xffffffffu, 0u};
+        SPHGB_CUDA(cudaMemcpy(ctx->d_check, init, sizeof(init), cudaMemcpyHostToDevice));
+    }
     return SPHGB_OK;
 }
 
@@ -1373,6 +1572,22 @@ std::mutex g_noalloc_mutex;
 constexpr int kNoAllocMaxDevices = 64;
 NoAllocScratch* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
+// Writes the call's scene descriptor and particle range into the shared
+// array and clears its counters.  The values travel as kernel arguments, which
+// are copied when the launch is enqueued, so no host buffer has to outlive
+// this call (a memcpy from the caller's stack would read it later).
+__global__ void k_noalloc_setup(NoAllocScratch* S, SceneDev scene, int n) {
+    if (threadIdx.x == 0) {
+        S->scene = scene;
+        S->pbegin[0] = 0;
+        S->pbegin[1] = n;
+        S->counters[0] = 0;
+        S->counters[1] = 0;
+    }
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 int noalloc_scratch(NoAllocScratch** out) {
     int dev = 0;
     SPHGB_CUDA(cudaGetDevice(&dev));
@@ -1413,19 +1628,26 @@ extern "C" int sphgb_organize_voxels_noalloc(const SphgbSceneParams* scene, cons
     if (n > 0 && (!d_pos || !d_vel || !d_pid || !d_pos_out || !d_vel_out || !d_pid_out))
         return fail(SPHGB_ERR_INVALID, "null buffer");
     if (!d_voxel_start || !d_voxel_count) return fail(SPHGB_ERR_INVALID, "null voxel table");
+    // the kernels move positions and velocities as float4 and the voxel table
+    // in 16-byte quads: a sub-allocated buffer must keep that alignment
+    const void* bufs[] = {d_pos, d_vel, d_pid, d_pos_out, d_vel_out, d_pid_out, d_voxel_start,
+                          d_voxel_count};
+    const char* names[] = {"d_pos", "d_vel", "d_pid", "d_pos_out", "d_vel_out", "d_pid_out",
+                           "d_voxel_start", "d_voxel_count"};
+    for (int i = 0; i < 8; ++i)
+        if (!aligned16(bufs[i]))
+            return fail(SPHGB_ERR_INVALID, std::string(names[i]) + " is not 16-byte aligned");
     NoAllocScratch* S = nullptr;
     rc = noalloc_scratch(&S);
     if (rc) return rc;
     d.p_begin = 0;
     d.p_count = n;
     d.v_begin = 0;
-    const int32_t pbegin[2] = {0, n};
     cudaStream_t st = as_stream(stream);
     // the scene descriptor and the counters live in the shared array too: a
     // later call overwrites them, so calls that overlap on the GPU race
-    SPHGB_CUDA(cudaMemcpyAsync(&S->scene, &d, sizeof(SceneDev), cudaMemcpyHostToDevice, st));
-    SPHGB_CUDA(cudaMemcpyAsync(S->pbegin, pbegin, sizeof(pbegin), cudaMemcpyHostToDevice, st));
-    SPHGB_CUDA(cudaMemsetAsync(S->counters, 0, sizeof(S->counters), st));
+    k_noalloc_setup<<<1, 32, 0, st>>>(S, d, n);
+    SPHGB_CUDA(cudaGetLastError());
     const int v_total = d.v_count + 1;
     SPHGB_CUDA(cudaMemsetAsync(d_voxel_count, 0, sizeof(int32_t) * v_total, st));
     if (n == 0) {

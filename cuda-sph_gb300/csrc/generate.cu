@@ -135,9 +135,11 @@ k_point_field(const float* __restrict__ pos, int stride, const float* __restrict
     }
 }
 
+// grid-stride launches: at most 64 blocks per SM
 int grid_for(int64_t n) {
     const int64_t b = (n + kBlock - 1) / kBlock;
-    return (int)(b < 152 * 64 ? b : 152 * 64);
+    const int64_t top = (int64_t)device_sm_count() * 64;
+    return (int)(b < top ? b : top);
 }
 
 }  // namespace

@@ -369,7 +369,8 @@ cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int3
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid) {
     if (L.n == 0) return cudaSuccess;
     // one block per SM: enough for the rare big voxels, idle blocks exit at once
-    k_sort_big<<<152, kSortThreads, 0, L.stream>>>(big_list, big_count, vstart, vcount, tmp_pid);
+    k_sort_big<<<device_sm_count(), kSortThreads, 0, L.stream>>>(big_list, big_count, vstart,
+                                                                 vcount, tmp_pid);
     return cudaGetLastError();
 }
 

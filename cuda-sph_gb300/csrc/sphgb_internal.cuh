@@ -431,6 +431,11 @@ struct RareList {
 };
 
 // ---- launchers (host) -----------------------------------------------------
+// Streaming multiprocessors of the current device, queried once per device
+// ordinal (cudaDevAttrMultiProcessorCount) and cached; persistent and
+// one-block-per-SM grids are sized from it.
+int device_sm_count();
+
 struct Launch {
     const SceneDev* scenes;     // device array
     const int32_t* pbegin;      // device, n_scenes + 1

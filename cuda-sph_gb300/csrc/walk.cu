@@ -639,7 +639,7 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
 // particles with every path.  The per-particle arithmetic is the same in all
 // three: the results are identical.
 constexpr int kForceAll = 0, kForceLean = 1, kForceRare = 2;
-constexpr int kRareBlocks = 152;   // kForceRare grid (one block per SM)
+// kForceRare grid: one block per SM (device_sm_count())
 
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
 // (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
@@ -807,7 +807,8 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
     if (L.n == 0) return cudaSuccess;
     // persistent grid: up to 4 blocks of 8 warps per SM, warps take tasks in turn
     int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
-    if (blocks > 152 * 4) blocks = 152 * 4;
+    const int top = device_sm_count() * 4;
+    if (blocks > top) blocks = top;
     auto kernel = L.layout == 1 ? k_density_wc<1> : L.layout == 2 ? k_density_wc<2> : k_density_wc<0>;
     kernel<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
                                                    vstart, vcount, rho, fin, nbr, tasks, task_count,
@@ -864,7 +865,7 @@ cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const f
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        k_integrate<false, kRange, kForceRare><<<kRareBlocks, kBlock, 0, L.stream>>>(
+        k_integrate<false, kRange, kForceRare><<<device_sm_count(), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
     } else {

@@ -10,7 +10,9 @@ voxel and neighbour decisions.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -20,6 +22,9 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libsphgb.so")
+# what the library was built on and with: a library built elsewhere (another
+# machine type, other flags) is never taken as up to date
+STAMP_PATH = os.path.join(BUILD_DIR, "libsphgb.stamp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
@@ -42,15 +47,25 @@ def _deps():
         os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB_PATH):
+def _stamp(flags) -> str:
+    h = hashlib.sha256()
+    for src in sorted(_deps()):
+        with open(src, "rb") as f:
+            h.update(os.path.basename(src).encode() + b"\0" + f.read())
+    return f"{platform.machine()} {' '.join(flags)} {h.hexdigest()}"
+
+
+def up_to_date(extra_flags=None) -> bool:
+    """The library exists and was built here, from these sources, with
+    these flags (not merely newer than the sources)."""
+    if not os.path.exists(LIB_PATH) or not os.path.exists(STAMP_PATH):
         return False
-    t = os.path.getmtime(LIB_PATH)
-    return all(os.path.getmtime(p) <= t for p in _deps())
+    with open(STAMP_PATH) as f:
+        return f.read() == _stamp(NVCC_FLAGS + list(extra_flags or []))
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
-    if not force and up_to_date():
+    if not force and up_to_date(extra_flags):
         return LIB_PATH
     nvcc = _nvcc()
     os.makedirs(BUILD_DIR, exist_ok=True)
@@ -80,6 +95,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)
     os.replace(tmp, LIB_PATH)
+    with open(STAMP_PATH, "w") as f:
+        f.write(_stamp(flags))
     return LIB_PATH
 
 

@@ -15,6 +15,9 @@ MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
 DENSITY_WARP, DENSITY_THREAD = 0, 1
 HOST_ORDER_AUTO, HOST_ORDER_SLOT, HOST_ORDER_PARTICLE = 0, 1, 2
+# checked-mode bits of the error word (sphgb_ctx_set_checks)
+CHECK_NONFINITE_INPUT, CHECK_OUT_OF_DOMAIN, CHECK_VOXEL_TABLE = 1, 2, 4
+CHECK_NEIGHBOUR_LIST, CHECK_NONFINITE_OUTPUT = 8, 16
 
 ERRORS = {
     -1: "SPHGB_ERR_INVALID",
@@ -98,6 +101,9 @@ SIGNATURES = [
     ("sphgb_ctx_set_host_order", _I, [_VP, _I]),
     ("sphgb_ctx_conservation", _I, [_VP, _VP, _VP]),
     ("sphgb_ctx_neighbour_counts", _I, [_VP, _VP, _VP, _VP]),
+    ("sphgb_ctx_step_neighbours", _I, [_VP, _VP, _VP, _VP]),
+    ("sphgb_ctx_set_checks", _I, [_VP, _I]),
+    ("sphgb_ctx_check_word", _I, [_VP, C.POINTER(C.c_uint32), _I, _VP]),
     ("sphgb_assign_voxels", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_organize_voxels", _I, [_VP] + [_VP] * 10 + [_VP]),
     ("sphgb_organize_voxels_noalloc", _I, [C.POINTER(SceneParams)] + [_VP] * 9),

@@ -256,6 +256,30 @@ class SceneBatch:
                    self._stream(stream))
         return cap[:self.n].cpu().numpy(), unc[:self.n].cpu().numpy()
 
+    def step_neighbours(self, stream=None):
+        """The latest step's neighbour lists as the force pass read them:
+        (list (N, 32) int32 of scene-local particle ids in walk order, self
+        left out, -1 padded; count (N,) int32, -1 above 32), original order,
+        as device tensors (see sphgb_ctx_step_neighbours)."""
+        torch = self._torch
+        n = max(self.n, 1)
+        lst = torch.empty((n, 32), dtype=torch.int32, device=self.device)
+        cnt = torch.empty((n,), dtype=torch.int32, device=self.device)
+        _capi.call("sphgb_ctx_step_neighbours", self._ctx, lst.data_ptr(), cnt.data_ptr(),
+                   self._stream(stream))
+        return lst[:self.n], cnt[:self.n]
+
+    def set_checks(self, enable: bool = True) -> None:
+        """Checked mode: validate every later step into the error word."""
+        _capi.call("sphgb_ctx_set_checks", self._ctx, 1 if enable else 0)
+
+    def check_word(self, clear: bool = False, stream=None):
+        """(bits, smallest flagged original index or None, flagged
+        particle-steps) of checked mode; synchronises the stream."""
+        w = (C.c_uint32 * 3)()
+        _capi.call("sphgb_ctx_check_word", self._ctx, w, 1 if clear else 0, self._stream(stream))
+        return int(w[0]), (None if w[1] == 0xFFFFFFFF else int(w[1])), int(w[2])
+
     def compute_next_state_host(self, pos, vel, pos_out=None, vel_out=None, rho_out=None):
         """One step through the host-buffer entry point (one-scene batches)."""
         pos = np.ascontiguousarray(pos, dtype=np.float64)

@@ -195,6 +195,44 @@ int sphgb_ctx_conservation(SphgbCtx* ctx, double* d_out, void* stream);
 int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_uncapped,
                                void* stream);
 
+/* The neighbour lists of the latest step of the context (sphgb_ctx_step or
+ * sphgb_compute_next_state_host), as that step's density pass recorded them
+ * and its force pass read them.  Row i (original particle order, scenes
+ * concatenated; 32 int32 per particle) holds particle i's neighbours other
+ * than itself in the reference's walk order, that is get_neighbours'
+ * capped list (voxel_kernels.py:30-85) with the particle itself taken out, as
+ * scene-local particle ids, -1 padded.  d_count[i] is their number, or -1
+ * when there were more than 32 (a scene with no cap; that row is all -1).
+ * Either pointer may be NULL.  SPHGB_ERR_STATE until a step has run, and
+ * again after sphgb_ctx_neighbour_counts or a reconfiguration, which re-sort
+ * the context's buffers. */
+int sphgb_ctx_step_neighbours(SphgbCtx* ctx, int32_t* d_list, int32_t* d_count, void* stream);
+
+/* Checked mode (off by default; no cost when off).  With enable != 0 every
+ * later step runs one more kernel that validates what the step read and
+ * wrote and ORs these bits into the context's error word.  The reference
+ * leaves these cases undefined (voxel ids of particles outside the box,
+ * voxel_kernels.py:10-17 and :89-105; never-written walk voxels and reads
+ * past voxel_begin, :44, :64-65, :70); this library defines its behaviour
+ * there (clamped voxel coordinates, an overflow entry for non-finite
+ * positions) and the word reports that it happened.  The check
+ * compares indices with their ranges before it uses them: bad data sets
+ * bits, it never faults.  Toggling drops the context's captured graphs. */
+enum {
+    SPHGB_CHECK_NONFINITE_INPUT = 1,   /* a position or velocity of the step's input is NaN/inf */
+    SPHGB_CHECK_OUT_OF_DOMAIN = 2,     /* a finite position outside [0, space_size) */
+    SPHGB_CHECK_VOXEL_TABLE = 4,       /* a slot outside its voxel's range, ids out of order */
+    SPHGB_CHECK_NEIGHBOUR_LIST = 8,    /* a list entry out of the scene, self, beyond h, or a
+                                          count beyond the cap */
+    SPHGB_CHECK_NONFINITE_OUTPUT = 16  /* density or next position/velocity is NaN/inf */
+};
+int sphgb_ctx_set_checks(SphgbCtx* ctx, int enable);
+/* Reads the error word into h_word[3] = {bits, smallest original index of a
+ * flagged particle (0xffffffff if none), flagged particle-steps}; with clear
+ * != 0 resets it.  Synchronises the stream.  All zero (and 0xffffffff) when
+ * checked mode was never enabled. */
+int sphgb_ctx_check_word(SphgbCtx* ctx, uint32_t* h_word, int clear, void* stream);
+
 /* ---- stages (each launches the same kernels sphgb_ctx_step uses) ------- */
 
 /* assign_voxels_to_particles_kernel (voxel_kernels.py:89-105): voxel id of
@@ -226,7 +264,9 @@ int sphgb_organize_voxels(SphgbCtx* ctx, const float* d_pos, const float* d_vel,
  * current; make it before any stream capture.  Every call shares the array and
  * it keeps the last call's contents: calls that overlap on the GPU (other
  * streams, other threads) race.  Outputs as sphgb_organize_voxels; the voxel
- * table has ceil dims + 1 entries. */
+ * table has ceil dims + 1 entries.  Every buffer must be 16-byte aligned
+ * (positions and velocities move as float4, the voxel table in int4 quads):
+ * SPHGB_ERR_INVALID names the first one that is not, before any GPU work. */
 int sphgb_organize_voxels_noalloc(const SphgbSceneParams* scene, const float* d_pos,
                                   const float* d_vel, const int32_t* d_pid, float* d_pos_out,
                                   float* d_vel_out, int32_t* d_pid_out, int32_t* d_voxel_start,

@@ -70,6 +70,27 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lib):
     assert "ctx is null" in _capi.last_error()
 
 
+def test_noalloc_refuses_misaligned_buffers_without_a_gpu(lib):
+    """The allocation-free voxel sort moves positions and velocities as float4
+    and the voxel table in int4 quads, so each buffer must be 16-byte aligned.
+    The check runs before any CUDA call: the addresses here are never touched."""
+    from sphgb import scenes
+    from sphgb.device import scene_params
+    spec, _ = scenes.config0()
+    sp = scene_params(spec)
+    base = 0x10000000
+    good = [base + 0x100000 * k for k in range(8)]
+    names = ["d_pos", "d_vel", "d_pid", "d_pos_out", "d_vel_out", "d_pid_out", "d_voxel_start",
+             "d_voxel_count"]
+    for i, name in enumerate(names):
+        for off in (4, 8, 12):
+            bufs = list(good)
+            bufs[i] += off
+            rc = lib.sphgb_organize_voxels_noalloc(C.byref(sp), *bufs, None)
+            assert rc == -1, (name, off, rc)
+            assert name in _capi.last_error() and "16-byte" in _capi.last_error()
+
+
 def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     monkeypatch.setattr(_capi, "_lib", None)
     monkeypatch.setattr(_capi, "lib_path", lambda: str(tmp_path / "missing.so"))

@@ -1,17 +1,68 @@
-"""The benchmark's own scene at full size: the 4,194,304-particle dam-break box
-(spacing 0.005, h 0.0112, [0,2]^3 box, a 5.7 M-voxel table).  One fused step
-against the FP64 oracle's step of the same input over every particle; the
-fused step (warp-cooperative density pass, forces over its neighbour list)
-against the stage-by-stage path (thread walks) bit for bit; and the
-host-buffer entry point against the device-resident path bit for bit, in both
-force-pass orders."""
+"""The benchmark scenes at their full sizes against the FP64 oracle.
+
+The 4,194,304-particle dam-break box (spacing 0.005, h 0.0112, [0,2]^3 box,
+a 5.7 M-voxel table), the headline workload:
+  * neighbour structure bit for bit over every particle: voxel ids, the sorted
+    (voxel, particle id) order, the voxel table, every ordered capped list,
+    capped and uncapped counts (the stage path, voxel_kernels.py:10-105 and
+    voxel_sph_strategy.py:84-107);
+  * the fused step's own neighbour rows, as its density pass recorded them
+    and its force pass read them: each equals the oracle's capped list with
+    the particle itself taken out;
+  * density, pressure and viscosity terms, next velocity and position per
+    particle within the bounds of the small cases (test_gpu_parity's module
+    docstring);
+  * the fused step bit for bit against the stage path, and the host-buffer
+    entry point bit for bit against the device path in both force-pass orders.
+
+The 262,144-particle pipe flow's start state (~133 particles per voxel, the
+density pass's dense-walk path and the FP64 pipe wall response): the same
+structure checks; particles whose wall response did not fire within the
+small-case bounds; those where it fired within 1e-3 of max(|x|, h) and of
+|v| + bound, except for a budget of 1e-4 of the particles (26) that may land
+on the other side of a wall decision (an FP32 and an FP64 velocity differing
+in the last bits can put x + v dt on either side of the pipe wall or the
+segment boundary, after which the two respawn or reflect differently).
+"""
 import numpy as np
 import pytest
 
 from gpu_util import run_stages, torch_cuda
 from oracle import ref
+from test_gpu_parity import (check_step, check_structure, oracle_step_dict, pipe_collided,
+                             rho_one, step_errors, TOL_RHO, TOL_TERM)
 
 pytestmark = pytest.mark.gpu
+
+WALL_FLIP_BUDGET = 1e-4     # fraction of particles
+
+
+def _fused(spec, st, step=0):
+    """One fused step (SceneBatch) from the given state: (state after the step,
+    the step's neighbour rows, their counts)."""
+    torch_cuda()
+    from sphgb.device import SceneBatch
+    b = SceneBatch([spec])
+    b.load_states([st])
+    if step:
+        b.steps.fill_(step)
+    b.step(1)
+    out = b.states()[0]
+    lst, cnt = (t.cpu().numpy() for t in b.step_neighbours())
+    b.close()
+    return out, lst, cnt
+
+
+def _lists_without_self(lst):
+    """Capped lists (self included, -1 padded) with each row's own index
+    removed, entries kept in walk order, -1 padded; and the entry counts."""
+    n = len(lst)
+    keep = (lst >= 0) & (lst != np.arange(n, dtype=lst.dtype)[:, None])
+    order = np.argsort(~keep, axis=1, kind="stable")
+    out = np.take_along_axis(lst, order, axis=1)
+    k = keep.sum(1)
+    out[np.arange(lst.shape[1])[None, :] >= k[:, None]] = -1
+    return out, k
 
 
 @pytest.fixture(scope="module")
@@ -23,49 +74,159 @@ def config2():
 
 
 @pytest.fixture(scope="module")
-def fused(config2):
-    torch_cuda()
-    from sphgb.device import SceneBatch
+def oracle2(config2):
     spec, st = config2
-    b = SceneBatch([spec])
-    b.load_states([st])
-    b.step(1)
-    out = b.states()[0]
-    b.close()
-    return out
+    return oracle_step_dict(spec, np.asarray(st.position, dtype=np.float64),
+                            np.asarray(st.velocity, dtype=np.float64))
 
 
-def test_full_size_step_matches_oracle(config2, fused):
-    """Tolerances as for the small scenes: density 1e-5 relative, position 1e-6
-    absolute, velocity 2e-4 of the largest (the force is a difference of terms
-    of similar size, so a relative bound per particle means nothing)."""
+@pytest.fixture(scope="module")
+def stages2(config2):
     spec, st = config2
-    sp = ref.params_from_spec(spec)
-    pos, vel, rho = ref.step(sp, st.position, st.velocity, step_index=0)
-    assert np.all(np.isfinite(fused.density)) and np.all(np.isfinite(fused.position))
-    assert np.max(np.abs(fused.density - rho) / rho) < 1e-5
-    assert np.max(np.abs(fused.position - pos)) < 1e-6
-    assert np.max(np.abs(fused.velocity - vel)) < 2e-4 * (np.abs(vel).max() + 1.0)
+    return run_stages(spec, st.position, st.velocity, step=0)
 
 
-def test_full_size_fused_step_bit_identical_to_stages(config2, fused):
+@pytest.fixture(scope="module")
+def fused2(config2):
     spec, st = config2
-    g = run_stages(spec, st.position, st.velocity, step=0)
-    np.testing.assert_array_equal(fused.density, g["density"])
-    np.testing.assert_array_equal(fused.velocity, g["velocity_out"])
-    np.testing.assert_array_equal(fused.position, g["position_out"])
+    return _fused(spec, st)
+
+
+def test_full_size_neighbour_structure_bit_exact(config2, oracle2, stages2):
+    spec, st = config2
+    exp, _, _ = oracle2
+    g = stages2
+    n = spec.n
+    ok = np.ones(n, dtype=bool)
+    np.testing.assert_array_equal(g["sorted_pid"], exp["sorted_pid"])
+    nv = len(exp["count"])
+    assert nv == 179 ** 3
+    np.testing.assert_array_equal(g["count"][:nv], exp["count"])
+    assert g["count"][nv] == 0          # no particle in the overflow entry
+    occupied = exp["count"] > 0
+    np.testing.assert_array_equal(g["start"][:nv][occupied], exp["start"][occupied])
+    check_structure(g, exp, ok, "config2")
+    print(f"config2: {occupied.sum()} occupied voxels; neighbours capped "
+          f"{exp['neigh_count'].mean():.2f} uncapped {exp['neigh_count_uncapped'].mean():.2f}; "
+          f"{(exp['neigh_count_uncapped'] > 32).mean():.3f} over the cap")
+
+
+def test_full_size_fused_neighbour_rows_bit_exact(config2, oracle2, fused2):
+    """The rows the fused step's force pass read (sphgb_ctx_step_neighbours)
+    against the oracle's get_neighbours lists, every particle."""
+    exp, _, _ = oracle2
+    _, lst, cnt = fused2
+    want, k = _lists_without_self(exp["neigh_list"])
+    np.testing.assert_array_equal(cnt, k)
+    np.testing.assert_array_equal(lst, want)
+
+
+def test_full_size_step_matches_oracle(config2, oracle2, stages2):
+    """Per particle: density 1e-5, pressure and viscosity terms 2e-4 of their
+    term scale, next velocity and position within the bounds those give."""
+    spec, st = config2
+    exp, scales, sp = oracle2
+    ok = np.ones(spec.n, dtype=bool)
+    check_step(stages2, exp, ok, scales, sp.dt, "config2/step0", ext=list(sp.external_force),
+               h=sp.inf_r, rho_1=rho_one(spec))
+
+
+def test_full_size_fused_step_bit_identical_to_stages(fused2, stages2):
+    out, _, _ = fused2
+    g = stages2
+    np.testing.assert_array_equal(out.density, g["density"])
+    np.testing.assert_array_equal(out.velocity, g["velocity_out"])
+    np.testing.assert_array_equal(out.position, g["position_out"])
 
 
 @pytest.mark.parametrize("order", ["slot", "particle"])
-def test_full_size_host_entry_bit_identical_to_device_path(config2, fused, order):
+def test_full_size_host_entry_bit_identical_to_device_path(config2, fused2, order):
     torch_cuda()
     from sphgb import _capi
     from sphgb.device import SceneBatch
     spec, st = config2
+    out, _, _ = fused2
     host = SceneBatch([spec])
     host.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE}[order])
     pos, vel, rho = host.compute_next_state_host(st.position, st.velocity)
     host.close()
-    np.testing.assert_array_equal(pos, fused.position)
-    np.testing.assert_array_equal(vel, fused.velocity)
-    np.testing.assert_array_equal(rho, fused.density)
+    np.testing.assert_array_equal(pos, out.position)
+    np.testing.assert_array_equal(vel, out.velocity)
+    np.testing.assert_array_equal(rho, out.density)
+
+
+# ---- the pipe flow at its full size -----------------------------------------
+
+@pytest.fixture(scope="module")
+def config1():
+    from sphgb import scenes
+    spec, st = scenes.config1()
+    assert spec.params.particle_count == 262_144
+    return spec, st
+
+
+@pytest.fixture(scope="module")
+def oracle1(config1):
+    spec, st = config1
+    return oracle_step_dict(spec, np.asarray(st.position, dtype=np.float64),
+                            np.asarray(st.velocity, dtype=np.float64), step=0)
+
+
+@pytest.fixture(scope="module")
+def stages1(config1):
+    spec, st = config1
+    return run_stages(spec, st.position, st.velocity, step=0)
+
+
+def test_pipe_full_size_neighbour_structure_bit_exact(config1, oracle1, stages1):
+    spec, st = config1
+    exp, _, _ = oracle1
+    g = stages1
+    ok = np.ones(spec.n, dtype=bool)
+    np.testing.assert_array_equal(g["sorted_pid"], exp["sorted_pid"])
+    nv = len(exp["count"])
+    np.testing.assert_array_equal(g["count"][:nv], exp["count"])
+    occupied = exp["count"] > 0
+    np.testing.assert_array_equal(g["start"][:nv][occupied], exp["start"][occupied])
+    check_structure(g, exp, ok, "config1")
+    print(f"config1: neighbours capped {exp['neigh_count'].mean():.2f} uncapped "
+          f"{exp['neigh_count_uncapped'].mean():.1f}")
+
+
+def test_pipe_full_size_step_matches_oracle(config1, oracle1, stages1):
+    spec, st = config1
+    exp, scales, sp = oracle1
+    g = stages1
+    pos = np.asarray(st.position, dtype=np.float64)
+    wall = (pipe_collided(pos, exp["velocity_out"], exp["position_out"], sp.dt)
+            | pipe_collided(pos, g["velocity_out"], g["position_out"], sp.dt))
+    free = ~wall
+    e_rho, e_p, e_v, nv, nx = step_errors(g, exp, np.ones(spec.n, dtype=bool), scales, sp.dt,
+                                          list(sp.external_force), sp.inf_r, None, rho_one(spec))
+    assert e_rho < TOL_RHO and e_p < TOL_TERM and e_v < TOL_TERM, (e_rho, e_p, e_v)
+    # wall response did not fire: the small-case bounds
+    if free.any():
+        assert nv[free].max() <= 1.0 and nx[free].max() <= 1.0
+    # it fired: 1e-3 of the vector norms, except for the flip budget
+    _, _, _, wv, wx = step_errors(g, exp, wall, scales, sp.dt, list(sp.external_force), sp.inf_r,
+                                  wall, rho_one(spec))
+    over = (wv.max(axis=1) > 1.0) | (wx.max(axis=1) > 1.0)
+    budget = int(WALL_FLIP_BUDGET * spec.n)
+    print(f"config1: rho {e_rho:.1e} P {e_p:.1e} V {e_v:.1e}; wall response fired for "
+          f"{wall.sum()} of {spec.n}; {over.sum()} outside 1e-3 (budget {budget})")
+    assert over.sum() <= budget
+
+
+def test_pipe_full_size_fused_step(config1, oracle1, stages1):
+    """The fused pipe step (FP64 position accumulator, one-launch force pass):
+    bit for bit against the stage path, and its neighbour rows against the
+    oracle's lists."""
+    spec, st = config1
+    exp, _, _ = oracle1
+    out, lst, cnt = _fused(spec, st)
+    np.testing.assert_array_equal(out.density, stages1["density"])
+    np.testing.assert_array_equal(out.velocity, stages1["velocity_out"])
+    np.testing.assert_array_equal(out.position, stages1["position_out"])
+    want, k = _lists_without_self(exp["neigh_list"])
+    np.testing.assert_array_equal(cnt, k)
+    np.testing.assert_array_equal(lst, want)

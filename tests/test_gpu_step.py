@@ -155,45 +155,77 @@ def test_host_entry_particle_ranges_uneven_counts(shape):
 
 
 def test_trajectory_config0_200_steps():
-    """200 free-running steps of the 8,192-particle dam break against the FP64
-    oracle.  The reference's capped walk makes the dynamics chaotic (a pair
-    crossing r = h changes which particle is the 32nd neighbour), so FP32 and
-    FP64 trajectories separate over time; the tolerances are per phase:
-      step 10        every particle within 1e-5 of the oracle
-      step 50        99 % of particles within 1e-4, median within 1e-6
-      step 100       median within 1e-5
-      every check    mean density within 1 %, non-finite particles <= 1 %
-    """
+    """200 free-running fused steps of the 8,192-particle dam break, every
+    step pinned by a shadow step of the FP64 oracle: from the GPU's own state
+    before step k, the oracle computes step k, and the GPU's step k must match
+    it with the tolerances of a single step (test_gpu_parity): the neighbour
+    rows the step's force pass read and their counts bit for bit, density
+    1e-5, next velocity and position within the bounds of the term scales.
+    Particles whose box wall response fired on one side only (an FP32 and an
+    FP64 position on either side of a wall) may differ by the reflection; at
+    most 2 per step and 10 over the run.
+
+    The two trajectories themselves separate over time, because the
+    reference's capped walk makes the dynamics chaotic (a pair crossing r = h
+    changes which particle is the 32nd neighbour); their distance is printed
+    as information, with only loose statistical bounds."""
     torch_cuda()
     from sphgb.device import SceneBatch
+    from test_gpu_parity import oracle_step_dict, rho_one, step_errors
+    from test_gpu_full_size import _lists_without_self
     spec, st = _scenes()["config0"]
     sp = ref.params_from_spec(spec)
     b = SceneBatch([spec])
     b.load_states([st])
-    pos, vel = st.position.copy(), st.velocity.copy()
+    pos, vel = st.position.copy(), st.velocity.copy()     # free-running oracle
     n = len(pos)
+    space = np.asarray(sp.space_size[:])
+    cur = b.states()[0]
+    flips_total = 0
     for k in range(200):
-        pos, vel, rho = ref.step(sp, pos, vel, step_index=k)
+        # shadow: the oracle's step k from the GPU's own state
+        gpos = np.asarray(cur.position, dtype=np.float64)
+        gvel = np.asarray(cur.velocity, dtype=np.float64)
+        exp, scales, _ = oracle_step_dict(spec, gpos, gvel, step=k)
         b.step(1)
+        nxt = b.states()[0]
+        lst, cnt = (t.cpu().numpy() for t in b.step_neighbours())
+        ok = np.isfinite(gpos).all(1) & np.all((gpos >= 0) & (gpos < space), axis=1)
+        want, kk = _lists_without_self(exp["neigh_list"])
+        np.testing.assert_array_equal(cnt[ok], kk[ok], err_msg=f"step {k}")
+        np.testing.assert_array_equal(lst[ok], want[ok], err_msg=f"step {k}")
+        g = {"density": nxt.density, "velocity_out": nxt.velocity, "position_out": nxt.position}
+        for what in ("velocity_out", "position_out"):
+            fa, fb = np.isfinite(g[what][ok]), np.isfinite(exp[what][ok])
+            assert np.array_equal(fa, fb), (k, what, "non-finite pattern")
+        e_rho, _, _, nv, nx = step_errors(g, exp, ok, scales, sp.dt, list(sp.external_force),
+                                          sp.inf_r, None, rho_one(spec))
+        assert e_rho < 1e-5, (k, e_rho)
+        over = (nv.max(axis=1) > 1.0) | (nx.max(axis=1) > 1.0)
+        if over.any():
+            # only particles the wall response moved on one side may differ
+            x_in = gpos[ok][over]
+            free_g = np.all(np.abs(x_in + nxt.velocity[ok][over] * sp.dt
+                                   - nxt.position[ok][over]) <= 1e-6, axis=1)
+            free_o = np.all(np.abs(x_in + exp["velocity_out"][ok][over] * sp.dt
+                                   - exp["position_out"][ok][over]) <= 1e-6, axis=1)
+            assert not np.any(free_g & free_o), (k, "off-wall particle outside its bound")
+            flips_total += int(over.sum())
+            assert over.sum() <= 2, (k, int(over.sum()))
+        cur = nxt
+        # free-running comparison, information only
+        pos, vel, rho = ref.step(sp, pos, vel, step_index=k)
         step = k + 1
-        if step not in (1, 10, 50, 100, 150, 200):
-            continue
-        g = b.states()[0]
-        fin = np.isfinite(g.position).all(1) & np.isfinite(pos).all(1)
-        dx = np.linalg.norm(g.position - pos, axis=1)[fin]
-        med, p99, mx = np.median(dx), np.quantile(dx, 0.99), dx.max()
-        drho = abs(g.density.mean() - rho.mean()) / rho.mean()
-        print(f"step {step}: |dx| median {med:.2e} p99 {p99:.2e} max {mx:.2e}; "
-              f"mean rho rel diff {drho:.1e}; non-finite gpu {n - np.isfinite(g.position).all(1).sum()} "
-              f"oracle {n - np.isfinite(pos).all(1).sum()}")
-        assert drho < 1e-2
-        assert (~fin).sum() <= 0.01 * n
-        if step <= 10:
-            assert mx < 1e-5
-        elif step == 50:
-            assert p99 < 1e-4 and med < 1e-6
-        elif step == 100:
-            assert med < 1e-5
+        if step in (1, 10, 50, 100, 150, 200):
+            fin = np.isfinite(nxt.position).all(1) & np.isfinite(pos).all(1)
+            dx = np.linalg.norm(nxt.position - pos, axis=1)[fin]
+            drho = abs(nxt.density.mean() - rho.mean()) / rho.mean()
+            print(f"step {step}: shadow rho {e_rho:.1e}, vel/bound {nv.max():.2f}, "
+                  f"pos/bound {nx.max():.2f}; free-running |dx| median {np.median(dx):.2e} "
+                  f"max {dx.max():.2e}, mean rho rel diff {drho:.1e}, non-finite gpu "
+                  f"{n - np.isfinite(nxt.position).all(1).sum()}")
+            assert drho < 1e-2 and (~fin).sum() <= 0.01 * n
+    assert flips_total <= 10
     b.close()
 
 
