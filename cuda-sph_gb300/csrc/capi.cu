@@ -130,7 +130,7 @@ struct SphgbCtx {
     int32_t* big_count = nullptr;     // counters: [0] big voxels, [1] density tasks, [2] tasks taken,
                                       // [3 + r] deferred particles of force pass r (kCounters)
     int32_t* rare = nullptr;          // deferred particles of the force pass (RareList)
-    int2* tasks = nullptr;             // (voxel, first slot) per run of <= 32 slots
+    int2* tasks = nullptr;             // (voxel, first slot) per run of <= kTaskRun slots
     // the neighbour rows in nbr, pidB and posB are those of the latest step
     // (cleared by anything else that sorts into the B buffers)
     bool nbr_valid = false;
@@ -288,6 +288,11 @@ int build_scene(const SphgbSceneParams& p, int n_pipe_rows_total, SceneDev& d,
         if (nv > (int64_t)0x7fffffff) return fail(SPHGB_ERR_RANGE, "voxel table over 2^31 entries");
     }
     d.v_count = (int32_t)nv;
+    for (int a = 0; a < 2; ++a) {
+        const Udiv u = make_udiv((uint32_t)(d.tiled ? (a ? d.nt1 : d.nt0) : d.dims[a]));
+        d.div_m[a] = u.m;
+        d.div_s[a] = u.p;
+    }
     const float h = (float)p.inf_r;
     const double hd = (double)h;
     d.h = h;

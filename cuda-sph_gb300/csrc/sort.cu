@@ -314,7 +314,7 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
         r = lo;
     }
     const int d = st + r;
-    if (tasks && (r & 31) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
+    if (tasks && (r % kTaskRun) == 0) tasks[atomicAdd(task_count, 1)] = make_int2(vid, d);
     pid_out[d] = p;
     pos_out[d] = __ldg(pos + s);
     if (vel) vel_out[d] = __ldg(vel + s);   // null: velocities gathered later

@@ -51,7 +51,32 @@ struct SceneDev {
     int32_t nt0, nt1;           // tiles along x and y when tiled
     int32_t pad;
     uint64_t seed;
+    // the two divisors of a table index -> coordinates decode (nt0, nt1 when
+    // tiled, else dims[0], dims[1]) as multiply-shift reciprocals (see Udiv)
+    uint32_t div_m[2];
+    int32_t div_s[2];
 };
+
+// floor(n / d) for 0 <= n < 2^31 and a divisor 1 <= d < 2^31 given as
+// m = ceil(2^p / d), p = 31 + ceil(log2 d): with e = m - 2^p/d in [0, 1),
+// n m / 2^p = n/d + n e / 2^p and n e / 2^p < 2^31 / 2^p = 2^-ceil(log2 d)
+// <= 1/d, which never carries n/d past the next integer (Granlund and
+// Montgomery, PLDI 1994, division by invariant integers).  m < 2^32.
+struct Udiv {
+    uint32_t m;
+    int32_t p;
+    __host__ __device__ __forceinline__ int div(int n) const {
+        return (int)(((unsigned long long)(unsigned)n * m) >> p);
+    }
+};
+
+inline Udiv make_udiv(uint32_t d) {
+    int L = 0;
+    while ((1ull << L) < d) ++L;
+    const int p = 31 + L;
+    const unsigned long long m = ((1ull << p) + d - 1) / d;
+    return Udiv{(uint32_t)m, p};
+}
 
 // Table index of voxel (x, y, z) of a scene.  Row-major, x fastest (the
 // reference's compute_1d_idx, voxel_kernels.py:14-17, with the stride dims
@@ -120,6 +145,7 @@ __device__ __forceinline__ bool finite3(const float4& p) {
 }
 
 // ---- Kahan summation ------------------------------------------------------
+// s - c is the running sum; c the rounding error still to be taken off.
 struct Kahan {
     float s = 0.0f, c = 0.0f;
     __device__ __forceinline__ void add(float x) {
@@ -128,7 +154,19 @@ struct Kahan {
         c = __fsub_rn(__fsub_rn(t, s), y);
         s = t;
     }
+    // the sum of b's terms added after this one's: b.s, then b's pending -c
+    __device__ __forceinline__ void merge(const Kahan& b) {
+        add(b.s);
+        add(-b.c);
+    }
 };
+
+// The density sum of a particle runs in two compensated parts that are then
+// merged: its accepted list entries (walk order, the particle itself counted
+// in the position) below kSumSplit, and the rest.  The warp-cooperative pass
+// gives the two parts to two lanes; the thread-per-particle pass uses the
+// same split, so both give the same bits.
+constexpr int kSumSplit = 16;
 
 // ---- the 27-voxel walk ----------------------------------------------------
 // Scene geometry the walk needs, loaded once per thread into registers.
@@ -469,8 +507,11 @@ constexpr int kBigVoxel = 64;
 constexpr int kMinBigVoxel = 16;
 cudaError_t launch_sort_big(const Launch& L, const int32_t* big_list, const int32_t* big_count,
                             const int32_t* vstart, const int32_t* vcount, int32_t* tmp_pid);
-// tasks (optional): one (voxel, first slot) entry per run of up to 32 sorted
-// slots of a voxel, appended at task_count.  tmp_pid must be 16-byte aligned
+// Density tasks: one (voxel, first slot) entry per run of up to kTaskRun
+// sorted slots of a voxel; a warp of the density pass takes one task at a time.
+constexpr int kTaskRun = 16;
+// tasks (optional): one (voxel, first slot) entry per run of up to kTaskRun
+// sorted slots of a voxel, appended at task_count.  tmp_pid must be 16-byte aligned
 // with 4 entries of room past n (the rank count reads it in aligned quads).
 cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32_t* slot,
                                const int32_t* pid, const int32_t* tmp_pid, const int32_t* vstart,
@@ -483,7 +524,7 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
 cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel,
                            const int32_t* vstart, const int32_t* vcount, float* rho,
                            float4* fin, NbrList nbr);
-// the step's density pass: one warp per task (<= 32 particles of one voxel);
+// the step's density pass: one warp per task (<= kTaskRun particles of one voxel);
 // task_next: a zeroed counter from which the warps take the tasks
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
                               const int32_t* vstart, const int32_t* vcount, float* rho,

@@ -44,8 +44,9 @@ __device__ __forceinline__ void write_force_inputs(int s, const float4& pi, cons
 
 // One particle's density by a thread-private walk: the walk records neighbour
 // slots in row[k * stride] (k < kListCap), the sum runs afterwards in walk
-// order; with more neighbours than that the walk is repeated, summing.
-// fin (with vel) is optional.  kLayout: see walk().
+// order in the two parts of kSumSplit; with more neighbours than that the
+// walk is repeated, summing in one part.  fin (with vel) is optional.
+// kLayout: see walk().
 template <int kLayout>
 __device__ __forceinline__ void density_one(int s, const float4& pi, const SceneDev& sc,
                                             const float4* __restrict__ pos,
@@ -55,16 +56,21 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
                                             float* __restrict__ rho, float4* __restrict__ fin,
                                             const NbrList& nbr, int32_t* row, int stride) {
     const WalkGeom g = load_geom(sc);
-    int others = 0;
+    int others = 0, lo = 0;   // lo: neighbours in the first part of the sum
+    bool self_seen = false;
     walk<kLayout>(pi, g, vstart, vcount, pos, g.cap, [&](int j, float, float, float, float) {
         if (j != s) {
+            if (others + (self_seen ? 1 : 0) < kSumSplit) ++lo;
             if (others < kListCap) row[others * stride] = j;
             ++others;
+        } else {
+            self_seen = true;
         }
     });
     const float inv_h2 = 1.0f / sc.h2;
     Kahan acc;
     if (others <= kListCap) {
+        Kahan acc2;
 #pragma unroll 4
         for (int k = 0; k < others; ++k) {
             const float4 pj = __ldg(pos + row[k * stride]);
@@ -75,8 +81,9 @@ __device__ __forceinline__ void density_one(int s, const float4& pi, const Scene
             d2 = __fmaf_rn(dy, dy, d2);
             d2 = __fmaf_rn(dz, dz, d2);
             const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
-            acc.add(u * u * u);
+            if (k < lo) acc.add(u * u * u); else acc2.add(u * u * u);
         }
+        acc.merge(acc2);
         if (nbr.idx)
             for (int k = 0; k < others; ++k) nbr.idx[(size_t)s * kListCap + k] = row[k * stride];
     } else {
@@ -121,19 +128,20 @@ __device__ __forceinline__ float dist2(const float4& a, const float4& b) {
     return __fmaf_rn(dz, dz, d2);
 }
 
-// Warp-cooperative density pass of the step.  One warp per task: up to 32
-// particles of one voxel (tasks listed by the rank-gather).  The 27 walk
-// voxels of that voxel are laid end to end in walk order; each batch of 96
-// candidates is loaded coalesced, three per lane (a candidate's slot found
+// Warp-cooperative density pass of the step.  One warp per task: up to
+// kTaskRun particles of one voxel (tasks listed by the rank-gather).  The 27
+// walk voxels of that voxel are laid end to end in walk order; each batch of
+// 96 candidates is loaded coalesced, three per lane (a candidate's slot found
 // from voxel-boundary bit masks built with one warp OR-reduction per 32
 // candidates), and every home particle is
 // tested against the whole batch at once: a ballot gives its accepted
 // candidates in walk order and popc ranks them against the cap, so the
 // accepted set is exactly the reference's first MAX_NEIGHBOURS (self
-// included).  Then the density terms are computed with
-// one lane per list entry and summed in walk order with one lane per home
-// particle, the arithmetic of density_one: the results are bit-identical to
-// the thread-per-particle kernel.
+// included).  Each accepted entry keeps its slot and its squared distance.
+// Then the density terms are computed from those distances with one lane per
+// list entry and summed in walk order with one lane per home particle, the
+// arithmetic of density_one: the results are bit-identical to the
+// thread-per-particle kernel.
 constexpr int kWcWarps = 8;
 // list entry of the particle itself once entries hold density terms: a NaN
 // bit pattern, which no term (a cube of a finite number) takes
@@ -168,16 +176,23 @@ __device__ __forceinline__ unsigned reach_mask(const float4& p, int vx, int vy, 
     return m;
 }
 
+// Per warp.  An accepted entry is its slot and its squared distance (int
+// bits), the distance the candidate loop decided on, so the density term
+// needs no second gather of the neighbour's position.  Phase (a) replaces the
+// distance with the term (kSelfTerm for the particle itself).  Rows are 33
+// words apart: phase (b) reads one row per lane without bank conflicts.
+static_assert(kTaskRun <= 16 && kTaskRun <= kSumSplit, "phase (b) gives each home two lanes");
 struct WcShared {
-    float4 home[32];
-    int32_t list[32][kWcList + 1];   // +1: row stride 33 words, no bank conflicts
+    float4 home[kTaskRun];
+    int32_t slot[kTaskRun][kWcList + 1];
+    int32_t dd[kTaskRun][kWcList + 1];
     int32_t off[27];    // first slot - first walk index of each non-empty walk voxel, by rank
 };
 
 // The candidate loop of k_density_wc for one task: batches of kWcBatch
 // candidates in walk order, each tested against every home particle still
-// below the cap.  Accepted slots go to S.list[i] in walk order and the counts
-// to cnt (lane i: home particle i).  Lane k < 27 holds walk voxel k's first
+// below the cap.  Accepted entries go to S.slot[i] and S.dd[i] in walk order
+// and the counts to cnt (lane i: home particle i).  Lane k < 27 holds walk voxel k's first
 // walk index Pk and member count ck.  kCull: a home particle skips the batches
 // that lie wholly in walk voxels outside its reach mask.
 template <bool kCull>
@@ -243,7 +258,7 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
                 band_seen |= !acc && d2 <= h2_hi;
                 const unsigned m = __ballot_sync(full, acc);
                 const int ru = r + __popc(m & lt);
-                if (acc && ru < cap) S.list[i][ru] = sj[u];
+                if (acc && ru < cap) { S.slot[i][ru] = sj[u]; S.dd[i][ru] = __float_as_int(d2); }
                 r += __popc(m);
             }
             if (lane == i) cnt = r;
@@ -262,7 +277,7 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
                         acc = within_exact(ph.x, ph.y, ph.z, pj[u].x, pj[u].y, pj[u].z, h_d);
                     const unsigned m = __ballot_sync(full, acc);
                     const int ru = r + __popc(m & lt);
-                    if (acc && ru < cap) S.list[i][ru] = sj[u];
+                    if (acc && ru < cap) { S.slot[i][ru] = sj[u]; S.dd[i][ru] = __float_as_int(d2); }
                     r += __popc(m);
                 }
                 if (lane == i) cnt = r;
@@ -301,7 +316,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         const int vid = task.x, d0 = task.y;
         const SceneDev& sc = scenes[scene_of(d0, pbegin, n_scenes)];
         const int vst = __ldg(vstart + vid), vc = __ldg(vcount + vid);
-        const int c_t = min(32, vst + vc - d0);
+        const int c_t = min(kTaskRun, vst + vc - d0);
         const int s = d0 + lane;
         const bool home = lane < c_t;
         const float4 pi = home ? __ldg(pos + s) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -310,26 +325,29 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home)
+            if (home)   // S.slot[lane] serves as its row buffer
                 density_one<kLayout>(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
-                                     &S.list[lane][0], 1);
+                                     &S.slot[lane][0], 1);
             __syncwarp();
             continue;
         }
         if (home) S.home[lane] = pi;
         // the 27 walk voxels (voxel_kernels.py:46-61 order), from the table coords
         const int tiled = kLayout == 2 ? sc.tiled : kLayout;
+        // index -> coordinates with the scene's multiply-shift reciprocals
+        const Udiv q0{sc.div_m[0], sc.div_s[0]}, q1{sc.div_m[1], sc.div_s[1]};
         int vx, vy, vz;
         if (tiled) {
             const int tl = local >> 6, in = local & 63;
-            vx = ((tl % sc.nt0) << 2) | (in & 3);
-            vy = (((tl / sc.nt0) % sc.nt1) << 2) | ((in >> 2) & 3);
-            vz = ((tl / (sc.nt0 * sc.nt1)) << 2) | (in >> 4);
+            const int r0 = q0.div(tl), r1 = q1.div(r0);
+            vx = ((tl - r0 * sc.nt0) << 2) | (in & 3);
+            vy = ((r0 - r1 * sc.nt1) << 2) | ((in >> 2) & 3);
+            vz = (r1 << 2) | (in >> 4);
         } else {
-            const int D0 = sc.dims[0], D1 = sc.dims[1];
-            vx = local % D0;
-            vy = (local / D0) % D1;
-            vz = local / (D0 * D1);
+            const int r0 = q0.div(local), r1 = q1.div(r0);
+            vx = local - r0 * sc.dims[0];
+            vy = r0 - r1 * sc.dims[1];
+            vz = r1;
         }
         int ck = 0, stk = 0;
         if (lane < 27) {
@@ -371,59 +389,69 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         else
             wc_candidates<false>(S, cnt, home, cap, M, Pk, ck, nzk, 0u, pos, h2_lo, h2_hi, h_d);
         __syncwarp();
-        // (a) one lane per list entry: the density term of every accepted pair
-        // replaces the entry (self gets kSelfTerm), and each particle's list
-        // row (neighbours other than itself, walk order) is written coalesced.
-        // Two particles' rows at a time, their position gathers issued together.
+        // (a) one lane per list entry: the density term of every accepted pair,
+        // from the squared distance its test used, replaces the distance (self
+        // gets kSelfTerm), and each particle's list row (neighbours other than
+        // itself, walk order) is written coalesced.  Two particles at a time.
         const float inv_h2 = 1.0f / sc.h2;
         for (int i0 = 0; i0 < c_t; i0 += 2) {
-            int jj[2];
-            float4 pq[2];
+            int2 en[2];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const int i = i0 + e;   // i0 even and < c_t <= 32: i <= 31
+                const int i = i0 + e;   // i0 even and < c_t <= kTaskRun: i < kTaskRun
                 const int na_i = i < c_t ? min(__shfl_sync(full, cnt, i), cap) : 0;
-                jj[e] = lane < na_i ? S.list[i][lane] : -1;
-                pq[e] = jj[e] >= 0 ? __ldg(pos + jj[e]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                en[e] = lane < na_i ? make_int2(S.slot[i][lane], S.dd[i][lane]) : make_int2(-1, 0);
             }
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 const int i = i0 + e;
                 if (i >= c_t) break;
                 const int si = d0 + i;
-                const int j = jj[e];
+                const int j = en[e].x;
                 const bool in = j >= 0;
                 const unsigned self = __ballot_sync(full, in && j == si);
                 if (in) {
                     int term = kSelfTerm;
                     if (j != si) {
-                        const float d2 = dist2(S.home[i], pq[e]);
-                        const float u = __fmaf_rn(-d2, inv_h2, 1.0f);
+                        const float u = __fmaf_rn(-__int_as_float(en[e].y), inv_h2, 1.0f);
                         term = __float_as_int(u * u * u);
                         if (nbr.idx)
                             nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
                     }
-                    S.list[i][lane] = term;
+                    S.dd[i][lane] = term;
                 }
             }
         }
         __syncwarp();
-        // (b) one lane per particle: the compensated sum in walk order, the
-        // arithmetic of density_one
-        if (home) {
-            const int na = min(cnt, cap);
+        // (b) two lanes per particle: lane i sums the entries of home i below
+        // kSumSplit, lane 16 + i the rest, each compensated in walk order,
+        // then lane i merges them: the arithmetic of density_one
+        {
+            const int ih = lane & 15;
+            const bool upper = lane >= 16;
+            const int na = min(__shfl_sync(full, cnt, ih), cap);
             Kahan acc;
             int others = 0;
-            for (int k = 0; k < na; ++k) {
-                const int term = S.list[lane][k];
-                if (term == kSelfTerm) continue;
-                acc.add(__int_as_float(term));
-                ++others;
+            if (ih < c_t) {
+                const int k1 = upper ? na : min(na, kSumSplit);
+                for (int k = upper ? kSumSplit : 0; k < k1; ++k) {
+                    const int term = S.dd[ih][k];
+                    if (term == kSelfTerm) continue;
+                    acc.add(__int_as_float(term));
+                    ++others;
+                }
             }
-            const float r = (acc.s * sc.w_const) * sc.mass;
-            rho[s] = r;
-            if (fin) write_force_inputs(s, pi, sc, vel, r, fin);
-            if (nbr.count) nbr.count[s] = others;
+            Kahan rest;
+            rest.s = __shfl_down_sync(full, acc.s, 16);
+            rest.c = __shfl_down_sync(full, acc.c, 16);
+            others += __shfl_down_sync(full, others, 16);
+            acc.merge(rest);
+            if (home) {
+                const float r = (acc.s * sc.w_const) * sc.mass;
+                rho[s] = r;
+                if (fin) write_force_inputs(s, pi, sc, vel, r, fin);
+                if (nbr.count) nbr.count[s] = others;
+            }
         }
         __syncwarp();
     }
