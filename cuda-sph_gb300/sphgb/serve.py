@@ -13,8 +13,10 @@ multi-scene context and advances all of them together, tick by tick:
 * the tick advances every active scene by K steps, K = the smallest number of
   steps any active scene still needs (at most max_tick_steps), so no scene is
   stepped past its request;
-* scenes whose steps are done retire: their state is copied out, memory frees
-  up and queued requests can be admitted.
+* scenes whose steps are done retire at the next tick boundary: their state
+  is copied out, memory frees up and queued requests can be admitted; the
+  retirements and admissions of one boundary are one re-pack (the running
+  state is exported once, the context reconfigured once).
 
 While the GPU runs a tick (kernel launches are asynchronous), the host
 generates and uploads the states of requests that arrived meanwhile, so their
@@ -79,10 +81,17 @@ class ServeStats:
     repacks: int
     max_active: int
     latencies: List[float] = field(default_factory=list)
+    gpu_s: float = 0.0          # device time of the ticks' steps (CUDA events)
+    repack_s: float = 0.0       # host wall time in re-packs (retirements with admissions)
 
     @property
     def throughput(self) -> float:
         return self.particle_steps / self.wall_s
+
+    @property
+    def gpu_busy(self) -> float:
+        """Fraction of the wall time the GPU spent stepping scenes."""
+        return self.gpu_s / self.wall_s if self.wall_s else 0.0
 
     def pct(self, q: float) -> float:
         return float(np.percentile(self.latencies, q)) if self.latencies else float("nan")
@@ -100,16 +109,24 @@ class SceneServer:
         self.used = 0
 
     # -- batch maintenance -----------------------------------------------
-    def _repack(self, admitted: List[Request]) -> None:
-        """Re-pack the batch: running scenes keep their device state and step
-        counters; admitted scenes start from their start state."""
+    def _rebuild(self, done: List[Request], admitted: List[Request], now: float) -> None:
+        """One membership change: finished scenes are copied out, the rest keep
+        their device state and step counters, admitted scenes start from their
+        start states.  The running state is exported once for both."""
         import torch
         dev = torch.device(self.device)
-        keep = self.active
+        keep = [r for r in self.active if r.remaining > 0]
         parts_pos, parts_vel, steps = [], [], []
-        if keep:
-            pos, vel, _ = self.batch.export_aos_f64()
+        if self.active and (done or admitted):
+            pos, vel, rho = self.batch.export_aos_f64()      # device, FP64, original order
             old_steps = self.batch.steps.clone()
+            for r in done:
+                k = self._index[r.rid]
+                off, n = self.batch.scene_offsets[k], self.batch.scene_sizes[k]
+                r.result = SimulationState(pos[off:off + n].cpu().numpy(),
+                                           vel[off:off + n].cpu().numpy(),
+                                           rho[off:off + n].cpu().numpy())
+                r.finished = now
             for r in keep:
                 k = self._index[r.rid]
                 off, n = self.batch.scene_offsets[k], self.batch.scene_sizes[k]
@@ -123,6 +140,9 @@ class SceneServer:
                                              device=dev).reshape(-1, 3))
             steps.append(torch.zeros(1, dtype=torch.int32, device=dev))
         reqs = keep + admitted
+        if not reqs:
+            self.batch_reset()
+            return
         specs = [r.spec for r in reqs]
         pos_all = torch.cat(parts_pos).contiguous()
         vel_all = torch.cat(parts_vel).contiguous()
@@ -136,22 +156,6 @@ class SceneServer:
         self.active = reqs
         self._index = {r.rid: k for k, r in enumerate(reqs)}
 
-    def _retire(self, now: float) -> List[Request]:
-        done = [r for r in self.active if r.remaining == 0]
-        if not done:
-            return []
-        pos, vel, rho = self.batch.export_aos_f64()          # device, FP64, original order
-        for r in done:
-            k = self._index[r.rid]
-            off, n = self.batch.scene_offsets[k], self.batch.scene_sizes[k]
-            r.result = SimulationState(pos[off:off + n].cpu().numpy(),
-                                       vel[off:off + n].cpu().numpy(),
-                                       rho[off:off + n].cpu().numpy())
-            r.finished = now
-            self.used -= footprint(r.spec)
-        self.active = [r for r in self.active if r.remaining > 0]
-        return done
-
     # -- the loop ------------------------------------------------------------
     def run(self, requests: List[Request], prepare: Callable[[Request], None] = None) -> ServeStats:
         """Serve `requests` (sorted by arrival time, seconds from now).
@@ -163,8 +167,11 @@ class SceneServer:
         queue: Deque[Request] = collections.deque()
         finished: List[Request] = []
         ticks = repacks = max_active = 0
+        gpu_s = repack_s = 0.0
         total = len(requests)
         ready = set()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
 
         def arrive(now):
             while schedule and schedule[0].arrival <= now:
@@ -174,6 +181,7 @@ class SceneServer:
                     ready.add(r.rid)
                 queue.append(r)
 
+        done: List[Request] = []          # finished in the last tick, not yet copied out
         while len(finished) < total:
             now = self.clock() - t0
             arrive(now)
@@ -184,12 +192,19 @@ class SceneServer:
                 r.remaining = r.steps
                 self.used += footprint(r.spec)
                 admitted.append(r)
-            if queue and not self.active and not admitted:
+            if queue and not self.active and not admitted and not done:
                 raise MemoryError(f"request {queue[0].rid} needs {footprint(queue[0].spec)} bytes, "
                                   f"over the {self.budget:.0f}-byte HBM budget")
-            if admitted:
-                self._repack(admitted)
+            if done or admitted:
+                # one re-pack per tick for retirements and admissions together
+                t_r = self.clock()
+                self._rebuild(done, admitted, now)
+                repack_s += self.clock() - t_r
                 repacks += 1
+                finished.extend(done)
+                done = []
+                if len(finished) == total:
+                    break
             if not self.active:
                 # idle: wait for the next arrival
                 if schedule:
@@ -197,7 +212,9 @@ class SceneServer:
                 continue
             max_active = max(max_active, len(self.active))
             k = min(self.max_tick, min(r.remaining for r in self.active))
+            ev0.record()
             self.batch.step(k)                       # asynchronous
+            ev1.record()
             # overlap: prepare requests that arrive while the GPU works
             if prepare is not None:
                 for r in schedule:
@@ -207,22 +224,19 @@ class SceneServer:
                         prepare(r)
                         ready.add(r.rid)
             torch.cuda.synchronize()
+            gpu_s += ev0.elapsed_time(ev1) / 1e3
             ticks += 1
             for r in self.active:
                 r.remaining -= k
-            done = self._retire(self.clock() - t0)
-            finished.extend(done)
-            if done and self.active:
-                # membership changed: re-pack the survivors (no admissions yet)
-                self._repack([])
-                repacks += 1
-            elif done:
-                self.batch_reset()
+            done = [r for r in self.active if r.remaining == 0]
+            for r in done:
+                self.used -= footprint(r.spec)     # its memory is free for admissions
         wall = self.clock() - t0
         ps = sum(r.spec.n * r.steps for r in finished)
         return ServeStats(requests=total, wall_s=wall, particle_steps=ps, ticks=ticks,
                           repacks=repacks, max_active=max_active,
-                          latencies=[r.latency for r in finished])
+                          latencies=[r.latency for r in finished], gpu_s=gpu_s,
+                          repack_s=repack_s)
 
     def batch_reset(self) -> None:
         self.active = []
