@@ -552,16 +552,30 @@ k_cons_partial(const SceneDev* __restrict__ scenes, const ConsChunk* __restrict_
     }
 }
 
+// One warp per scene over the scene's own chunks (contiguous, in scene
+// order): lane-strided partial sums, then a fixed shuffle tree.  The order
+// depends only on the scene's chunk count, so a scene gives the same sums
+// alone or batched.
 __global__ void k_cons_final(const ConsChunk* __restrict__ chunks, int n_chunks,
                              const double* __restrict__ partials, const SceneDev* __restrict__ scenes,
                              int n_scenes, double* __restrict__ out) {
-    const int si = blockIdx.x * blockDim.x + threadIdx.x;
+    const int si = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (si >= n_scenes) return;
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int c = 0; c < n_chunks; ++c) {
-        if (chunks[c].scene != si) continue;
-        for (int f = 0; f < 6; ++f) acc[f] += partials[(size_t)c * 6 + f];
+    // first chunk of the scene: lower bound of si in the chunks' scene ids
+    int lo = 0, hi = n_chunks;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (chunks[mid].scene < si) lo = mid + 1; else hi = mid;
     }
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = lo + lane; c < n_chunks && chunks[c].scene == si; c += 32)
+        for (int f = 0; f < 6; ++f) acc[f] += partials[(size_t)c * 6 + f];
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[f] += __shfl_down_sync(0xffffffffu, acc[f], o);
+    if (lane != 0) return;
     double* o = out + (size_t)si * kConsFields;
     o[0] = acc[0];
     o[1] = acc[1];
@@ -1276,7 +1290,7 @@ int sphgb_ctx_conservation(SphgbCtx* ctx, double* d_out, void* stream) {
         k_cons_partial<<<ctx->n_chunks, kConsThreads, 0, st>>>(ctx->d_scenes, ctx->d_chunks,
                                                                ctx->posA, ctx->velA, ctx->pos64A,
                                                                ctx->d_partials);
-    k_cons_final<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->d_chunks, ctx->n_chunks,
+    k_cons_final<<<blocks(ctx->n_scenes * 32, 128), 128, 0, st>>>(ctx->d_chunks, ctx->n_chunks,
                                                             ctx->d_partials, ctx->d_scenes,
                                                             ctx->n_scenes, d_out);
     SPHGB_CUDA(cudaGetLastError());

@@ -103,3 +103,41 @@ def test_reconfigure_and_tuning_keep_results():
             np.testing.assert_array_equal(getattr(got, f), getattr(want, f), err_msg=str(tuning))
     b.close()
     base.close()
+
+
+def test_batched_workload_every_scene_against_the_oracle():
+    """The batched workload at its full size (256 boxes, 1,024-65,536
+    particles each, one context): after one batched step, every scene's
+    neighbour rows and counts equal the FP64 oracle's capped lists bit for
+    bit, and its density is within 1e-5 (relative, per particle; the
+    small-case bound); its first step's conservation sums equal FP64 sums of
+    its own state."""
+    torch_cuda()
+    from sphgb import scenes
+    from sphgb.device import SceneBatch
+    from test_gpu_full_size import _lists_without_self
+    pairs = scenes.config3_specs(n_scenes=256, seed=3)
+    b = SceneBatch([p[0] for p in pairs])
+    b.load_states([p[1] for p in pairs])
+    b.step(1)
+    got = b.states()
+    lst, cnt = (t.cpu().numpy() for t in b.step_neighbours())
+    cons = b.conservation()
+    b.close()
+    worst = 0.0
+    for k, ((spec, st), g) in enumerate(zip(pairs, got)):
+        off = b.scene_offsets[k]
+        sp = ref.params_from_spec(spec)
+        spid, start, count = ref.organize(sp, ref.assign_voxels(sp, st.position))
+        want_l, _, _ = ref.neighbours(sp, st.position, spid, start, count)
+        rows, kk = _lists_without_self(want_l)
+        np.testing.assert_array_equal(cnt[off:off + spec.n], kk, err_msg=f"scene {k}")
+        np.testing.assert_array_equal(lst[off:off + spec.n], rows, err_msg=f"scene {k}")
+        rho = ref.density(sp, st.position, spid, start, count)
+        err = float(np.max(np.abs(g.density - rho) / rho))
+        worst = max(worst, err)
+        assert err < 1e-5, (k, err)
+        m = np.float64(np.float32(spec.constants.mass))
+        assert abs(cons[k][0] - m * spec.n) <= 1e-12 * m * spec.n
+        assert cons[k][7] == spec.n
+    print(f"256 scenes: density max rel err {worst:.1e}")
