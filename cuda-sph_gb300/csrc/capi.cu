@@ -1364,9 +1364,9 @@ int sphgb_ctx_check_word(SphgbCtx* ctx, uint32_t* h_word, int clear, void* strea
     h_word[0] = w[0];
     h_word[1] = w[1];
     h_word[2] = w[2];
-    if (clear) {
-        const uint32_t init[3] = {0u, 0xffffffffu, 0u};
-        SPHGB_CUDA(cudaMemcpy(ctx->d_check, init, sizeof(init), cudaMemcpyHostToDevice));
+    if (clear) {   // {0, 0xffffffff, 0}, ordered on the caller's stream
+        SPHGB_CUDA(cudaMemsetAsync(ctx->d_check, 0, 3 * sizeof(uint32_t), st));
+        SPHGB_CUDA(cudaMemsetAsync(ctx->d_check + 1, 0xff, sizeof(uint32_t), st));
     }
     return SPHGB_OK;
 }
