@@ -146,6 +146,9 @@ struct SphgbCtx {
     double* pos64A = nullptr;
     int32_t* scene_step = nullptr;
     bool bound = false;
+    // optional per-scene step limits (caller-owned device array, see
+    // sphgb_ctx_set_step_limits); null: no scene is frozen
+    const int32_t* step_limit = nullptr;
     // optional separate output of the step (the input state is then left untouched)
     float4* out_pos = nullptr;
     float4* out_vel = nullptr;
@@ -197,6 +200,10 @@ struct SphgbCtx {
         L.sort_block = sort_block;
         L.big_voxel = big_voxel;
         L.stream = st;
+        // the stage entry points step no scene counter: limits apply to the
+        // context's own step only
+        L.step_limit = ref_layout ? nullptr : step_limit;
+        L.scene_step = scene_step;
         return L;
     }
 };
@@ -396,9 +403,9 @@ __global__ void k_store_aos(const SceneDev* __restrict__ scenes, const int32_t* 
     if (rho_out) rho_out[i] = rho ? (double)rho[s] : 0.0;
 }
 
-__global__ void k_step_counter(int32_t* scene_step, int n_scenes) {
+__global__ void k_step_counter(int32_t* scene_step, int n_scenes, const int32_t* step_limit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_scenes) scene_step[i] += 1;
+    if (i < n_scenes && !(step_limit && scene_step[i] >= step_limit[i])) scene_step[i] += 1;
 }
 
 // values per sorted slot -> original particle order (scene offset + pid)
@@ -444,11 +451,14 @@ __global__ void k_check_step(const SceneDev* __restrict__ scenes, const int32_t*
                              const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
                              NbrList nbr, const float* __restrict__ rho,
                              const float4* __restrict__ pos_out, const float4* __restrict__ vel_out,
-                             uint32_t* __restrict__ word) {
+                             uint32_t* __restrict__ word, const int32_t* __restrict__ step_limit,
+                             const int32_t* __restrict__ scene_step) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const int si = scene_of(s, pbegin, n_scenes);
     const SceneDev& sc = scenes[si];
+    // a frozen scene keeps its slots (not voxel-sorted) and has no list rows
+    const bool frozen = scene_frozen(step_limit, scene_step, si);
     const float4 p = pos[s];
     uint32_t bits = 0;
     if (!finite3(p) || !finite3(vel[s])) bits |= SPHGB_CHECK_NONFINITE_INPUT;
@@ -467,17 +477,20 @@ __global__ void k_check_step(const SceneDev* __restrict__ scenes, const int32_t*
     }
     const int st = vstart[vid], c = vcount[vid];
     const int p_lo = sc.p_begin, p_hi = sc.p_begin + sc.p_count;
-    if (c <= 0 || st < p_lo || st + c > p_hi || s < st || s >= st + c)
+    if (frozen) {
+        // slots kept from an earlier step: nothing to check against the table
+    } else if (c <= 0 || st < p_lo || st + c > p_hi || s < st || s >= st + c) {
         bits |= SPHGB_CHECK_VOXEL_TABLE;
-    else if (vid != sc.v_begin + sc.v_count && s > st && !(pid[s - 1] < pid[s]))
+    } else if (vid != sc.v_begin + sc.v_count && s > st && !(pid[s - 1] < pid[s])) {
         bits |= SPHGB_CHECK_VOXEL_TABLE;
+    }
     const int myid = pid[s];
     if (myid < 0 || myid >= sc.p_count) bits |= SPHGB_CHECK_VOXEL_TABLE;
     // neighbour row: other particles of the same scene within h (guard band).
     // A row holds at most cap others: cap - 1 when the particle itself is
     // among the first cap accepted, cap when more than cap - 1 neighbours come
     // before it in walk order.
-    if (nbr.count) {
+    if (nbr.count && !frozen) {
         const int cnt = nbr.count[s];
         if (cnt < -1 || cnt > kListCap || (sc.cap <= kListCap && cnt > sc.cap)) {
             bits |= SPHGB_CHECK_NEIGHBOUR_LIST;
@@ -697,7 +710,8 @@ int enqueue_checks(SphgbCtx* c, cudaStream_t st) {
     k_check_step<<<blocks(c->n), kBlock, 0, st>>>(c->d_scenes, c->d_pbegin, c->n_scenes, c->n,
                                                   c->posB, c->velB, c->pidB, c->vstart, c->vcount,
                                                   c->nbr, c->rho, sep ? c->out_pos : c->posA,
-                                                  sep ? c->out_vel : c->velA, c->d_check);
+                                                  sep ? c->out_vel : c->velA, c->d_check,
+                                                  c->step_limit, c->scene_step);
     SPHGB_CUDA(cudaGetLastError());
     return SPHGB_OK;
 }
@@ -746,7 +760,8 @@ int enqueue_step(SphgbCtx* c, cudaStream_t st, cudaEvent_t* ev = nullptr,
     rc = enqueue_checks(c, st);
     if (rc) return rc;
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[6], st));
-    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes);
+    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st>>>(c->scene_step, c->n_scenes,
+                                                              c->step_limit);
     SPHGB_CUDA(cudaGetLastError());
     if (ev) SPHGB_CUDA(cudaEventRecord(ev[7], st));
     return SPHGB_OK;
@@ -859,6 +874,7 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     // the caller binds (new) state and outputs for the new layout
     c->bound = false;
     c->nbr_valid = false;
+    c->step_limit = nullptr;   // one entry per scene of the old layout
     c->posA = c->velA = nullptr;
     c->rho = nullptr;
     c->pidA = nullptr;
@@ -1256,7 +1272,8 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
         }
         rc = enqueue_checks(ctx, st);
         if (rc) return rc;
-        k_step_counter<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->scene_step, ctx->n_scenes);
+        k_step_counter<<<blocks(ctx->n_scenes, 128), 128, 0, st>>>(ctx->scene_step, ctx->n_scenes,
+                                                                    ctx->step_limit);
         SPHGB_CUDA(cudaGetLastError());
         SPHGB_CUDA(cudaEventRecord(e_done, st2));
         SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
@@ -1301,7 +1318,8 @@ int sphgb_ctx_neighbour_counts(SphgbCtx* ctx, int32_t* d_capped, int32_t* d_unca
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (!ctx->bound) return fail(SPHGB_ERR_STATE, "no state bound");
     cudaStream_t st = as_stream(stream);
-    const Launch L = ctx->launch(st);
+    Launch L = ctx->launch(st);
+    L.step_limit = nullptr;   // counts of every scene, frozen or not
     int rc = enqueue_organize(ctx, L, ctx->posA, ctx->velA, ctx->pidA,
                               ctx->any_pipe ? ctx->pos64A : nullptr, ctx->posB, ctx->velB,
                               ctx->pidB, ctx->any_pipe ? ctx->pos64B : nullptr, ctx->vstart,
@@ -1327,6 +1345,17 @@ int sphgb_ctx_step_neighbours(SphgbCtx* ctx, int32_t* d_list, int32_t* d_count, 
     k_export_neighbours<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                                            ctx->pidB, ctx->nbr, d_list, d_count);
     SPHGB_CUDA(cudaGetLastError());
+    return SPHGB_OK;
+}
+
+int sphgb_ctx_set_step_limits(SphgbCtx* ctx, const int32_t* d_limits) {
+    if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (d_limits != ctx->step_limit) {
+        // captured step graphs hold the old pointer
+        for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+        ctx->graphs.clear();
+    }
+    ctx->step_limit = d_limits;
     return SPHGB_OK;
 }
 

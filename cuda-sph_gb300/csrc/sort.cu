@@ -284,9 +284,22 @@ k_rank_gather(int n, const int32_t* __restrict__ cell, const int32_t* __restrict
               float4* __restrict__ pos_out, float4* __restrict__ vel_out,
               int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
               int2* __restrict__ tasks, int32_t* __restrict__ task_count, int big_voxel,
-              const int32_t* __restrict__ slot) {
+              const int32_t* __restrict__ slot, const int32_t* __restrict__ pbegin, int n_scenes,
+              const int32_t* __restrict__ step_limit, const int32_t* __restrict__ scene_step) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
+    if (step_limit && scene_frozen(step_limit, scene_step, scene_of(s, pbegin, n_scenes))) {
+        // frozen scene: every particle keeps its slot, no density task
+        pid_out[s] = pid[s];
+        pos_out[s] = __ldg(pos + s);
+        if (vel) vel_out[s] = __ldg(vel + s);
+        if (pos64) {
+            pos64_out[3 * s + 0] = pos64[3 * s + 0];
+            pos64_out[3 * s + 1] = pos64[3 * s + 1];
+            pos64_out[3 * s + 2] = pos64[3 * s + 2];
+        }
+        return;
+    }
     const int code = cell[s];
     const int vid = code < 0 ? ~code : code;
     const int p = pid[s];
@@ -385,7 +398,8 @@ cudaError_t launch_rank_gather(const Launch& L, const int32_t* cell, const int32
     k_rank_gather<<<(L.n + b - 1) / b, b, 0, L.stream>>>(L.n, cell, pid, tmp_pid, vstart, vcount,
                                                          pos, vel, pos64, pos_out, vel_out,
                                                          pid_out, pos64_out, tasks, task_count,
-                                                         L.big_voxel, slot);
+                                                         L.big_voxel, slot, L.pbegin, L.n_scenes,
+                                                         L.step_limit, L.scene_step);
     return cudaGetLastError();
 }
 

@@ -103,6 +103,14 @@ __device__ __forceinline__ int scene_of(int s, const int32_t* __restrict__ pbegi
     return lo;
 }
 
+// ---- per-scene step limits --------------------------------------------------
+// With step limits bound (sphgb_ctx_set_step_limits), a scene whose step
+// counter has reached its limit is frozen: a step leaves its state unchanged.
+__device__ __forceinline__ bool scene_frozen(const int32_t* __restrict__ limit,
+                                             const int32_t* __restrict__ step, int si) {
+    return limit && __ldg(step + si) >= __ldg(limit + si);
+}
+
 // ---- exact voxel coordinate ----------------------------------------------
 __device__ __forceinline__ int voxel_coord(float x, float vs, int dim) {
     if (!(x >= 0.0f)) return 0;                  // negative or NaN: first voxel
@@ -486,6 +494,11 @@ struct Launch {
     int big_voxel = 64;         // voxels above this many members are sorted per block
     int layout = 0;             // voxel tables: 0 all row-major, 1 all tiled, 2 mixed
     cudaStream_t stream;
+    // per-scene step limits and counters (device, n_scenes each); limits null:
+    // no scene is frozen.  A frozen scene's particles keep their slots in the
+    // sort, get no density task and are copied through by the force pass.
+    const int32_t* step_limit = nullptr;
+    const int32_t* scene_step = nullptr;
 };
 
 // cell[s] = voxel id, or ~id (negative) for a particle in its scene's overflow

@@ -109,11 +109,14 @@ __global__ void __launch_bounds__(kBlock)
 k_density(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
           int n, const float4* __restrict__ pos, const float4* __restrict__ vel,
           const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
-          float* __restrict__ rho, float4* __restrict__ fin, NbrList nbr) {
+          float* __restrict__ rho, float4* __restrict__ fin, NbrList nbr,
+          const int32_t* __restrict__ step_limit, const int32_t* __restrict__ scene_step) {
     __shared__ int32_t s_list[kListCap][kBlock];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const SceneDev& sc = scenes[scene_of(s, pbegin, n_scenes)];
+    const int si = scene_of(s, pbegin, n_scenes);
+    if (scene_frozen(step_limit, scene_step, si)) return;   // state and density stay
+    const SceneDev& sc = scenes[si];
     density_one<kLayout>(s, __ldg(pos + s), sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
                          &s_list[0][threadIdx.x], kBlock);
 }
@@ -686,7 +689,8 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             const int32_t* __restrict__ vcount, const int32_t* __restrict__ scene_step,
             NbrList nbr, float4* __restrict__ pos_out, float4* __restrict__ vel_out,
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
-            float4* __restrict__ force_out, PidRange range, RareList rare) {
+            float4* __restrict__ force_out, PidRange range, RareList rare,
+            const int32_t* __restrict__ step_limit) {
     // kForceRare: a grid-stride loop over the deferred particles; otherwise one
     // particle per thread (the body runs once)
     const int m_rare = kMode == kForceRare ? *rare.count : 0;
@@ -706,6 +710,29 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
         }
         const int si = scene_of(s, pbegin, n_scenes);
         const SceneDev& sc = scenes[si];
+        if (kMode != kForceRare && scene_frozen(step_limit, scene_step, si)) {
+            // frozen scene: the state is copied through unchanged (the sort
+            // kept its slots; its force records were not written this step)
+            const float4 p4 = __ldg(pos + s), v4 = __ldg(vel + s);
+            pos_out[s] = p4;
+            vel_out[s] = v4;
+            pid_out[s] = __ldg(pid + s);
+            double x64[3] = {p4.x, p4.y, p4.z};
+            if (kPipe && pos64_out) {
+                for (int a = 0; a < 3; ++a) {
+                    pos64_out[3 * s + a] = pos64[3 * s + a];
+                    if (sc.mode == 1) x64[a] = pos64[3 * s + a];
+                }
+            }
+            if (kRange) {
+                for (int a = 0; a < 3; ++a) range.pos[3 * (size_t)row + a] = x64[a];
+                range.vel[3 * (size_t)row + 0] = v4.x;
+                range.vel[3 * (size_t)row + 1] = v4.y;
+                range.vel[3 * (size_t)row + 2] = v4.z;
+            }
+            if (force_out) force_out[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            return;   // one particle per thread outside kForceRare
+        }
         // the particle's own force record holds its position and velocity too
         // (written from this state by the density pass, k_gather_vel or
         // k_force_inputs), so one 32-byte load serves for both
@@ -824,7 +851,8 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel
     if (L.n == 0) return cudaSuccess;
     auto kernel = L.layout == 1 ? k_density<1> : L.layout == 2 ? k_density<2> : k_density<0>;
     kernel<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
-                                                     vstart, vcount, rho, fin, nbr);
+                                                     vstart, vcount, rho, fin, nbr, L.step_limit,
+                                                     L.scene_step);
     return cudaGetLastError();
 }
 
@@ -886,21 +914,23 @@ cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const f
         k_integrate<true, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
-            RareList{});
+            RareList{}, L.step_limit);
     } else if (nbr.count && rare.count) {
         k_integrate<false, kRange, kForceLean><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
+            L.step_limit);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         k_integrate<false, kRange, kForceRare><<<device_sm_count(), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
-            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare);
+            vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
+            L.step_limit);
     } else {
         k_integrate<false, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
-            RareList{});
+            RareList{}, L.step_limit);
     }
     return cudaGetLastError();
 }

@@ -95,6 +95,7 @@ SIGNATURES = [
     ("sphgb_ctx_bind_output", _I, [_VP, _VP, _VP, _VP, _VP]),
     ("sphgb_ctx_load_aos_f64", _I, [_VP, _VP, _VP, _VP]),
     ("sphgb_ctx_store_aos_f64", _I, [_VP, _VP, _VP, _VP, _VP]),
+    ("sphgb_ctx_set_step_limits", _I, [_VP, _VP]),
     ("sphgb_ctx_step", _I, [_VP, _I, _I, _VP]),
     ("sphgb_ctx_step_profiled", _I, [_VP, _I, _VP, C.POINTER(C.c_float)]),
     ("sphgb_compute_next_state_host", _I, [_VP, _VP, _VP, _VP, _VP, _VP]),

@@ -73,6 +73,7 @@ class SceneBatch:
         self.device = torch.device(device)
         self._ctx = None
         self.out_pos = self.out_vel = self.out_pid = self.out_pos64 = None
+        self.step_limits = None
         self._configure(specs)
 
     def _tables(self, specs):
@@ -125,6 +126,7 @@ class SceneBatch:
             self.pid.data_ptr(), self.pos64.data_ptr(), self.steps.data_ptr()),
             "sphgb_ctx_bind_state")
         self.out_pos = self.out_vel = self.out_pid = self.out_pos64 = None
+        self.step_limits = None          # the context drops its limits on reconfiguration
 
     def reconfigure(self, specs: Sequence[SceneSpec], steps=None) -> None:
         """Replace the scenes, reusing the context's scratch where it fits.
@@ -225,6 +227,23 @@ class SceneBatch:
         return out
 
     # -- stepping and diagnostics ----------------------------------------
+    def set_step_limits(self, limits=None) -> None:
+        """Per-scene step limits (sphgb_ctx_set_step_limits): a sequence of one
+        step count per scene, or a device int32 tensor, or None to remove
+        them.  A scene whose step counter (self.steps) has reached its limit
+        is frozen: later steps leave it unchanged.  The tensor is kept as
+        self.step_limits; writing new values into it needs no new call."""
+        torch = self._torch
+        if limits is None:
+            self.step_limits = None
+            _capi.call("sphgb_ctx_set_step_limits", self._ctx, None)
+            return
+        t = torch.as_tensor(limits, dtype=torch.int32, device=self.device).contiguous()
+        if t.numel() != len(self.specs):
+            raise ValueError("one step limit per scene")
+        self.step_limits = t
+        _capi.call("sphgb_ctx_set_step_limits", self._ctx, t.data_ptr())
+
     def step(self, n_steps: int = 1, use_graph: bool = False, stream=None) -> None:
         _capi.call("sphgb_ctx_step", self._ctx, int(n_steps), 1 if use_graph else 0,
                    self._stream(stream))

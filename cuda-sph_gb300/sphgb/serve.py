@@ -10,9 +10,11 @@ multi-scene context and advances all of them together, tick by tick:
 * admitted scenes join the running batch: the context is re-packed (scratch
   buffers that are big enough are reused), running scenes keep their state
   and step counters on the device, new scenes' start states are copied in;
-* the tick advances every active scene by K steps, K = the smallest number of
-  steps any active scene still needs (at most max_tick_steps), so no scene is
-  stepped past its request;
+* the tick advances every active scene by up to K steps, K = the largest
+  number of steps any active scene still needs (at most max_tick_steps).  Each
+  scene's request is its step limit on the device
+  (sphgb_ctx_set_step_limits), so a scene that reaches it inside the tick is
+  frozen there and is never stepped past its request;
 * scenes whose steps are done retire at the next tick boundary: their state
   is copied out, memory frees up and queued requests can be admitted; the
   retirements and admissions of one boundary are one re-pack (the running
@@ -153,6 +155,8 @@ class SceneServer:
         else:
             self.batch.reconfigure(specs, steps=step_all)
         self.batch.load_aos_device(pos_all, vel_all, reset_steps=False)
+        # every scene stops at its request (step counters count from its start)
+        self.batch.set_step_limits([r.steps for r in reqs])
         self.active = reqs
         self._index = {r.rid: k for k, r in enumerate(reqs)}
 
@@ -211,7 +215,7 @@ class SceneServer:
                     time.sleep(max(0.0, min(schedule[0].arrival - (self.clock() - t0), 0.01)))
                 continue
             max_active = max(max_active, len(self.active))
-            k = min(self.max_tick, min(r.remaining for r in self.active))
+            k = min(self.max_tick, max(r.remaining for r in self.active))
             ev0.record()
             self.batch.step(k)                       # asynchronous
             ev1.record()
@@ -227,7 +231,7 @@ class SceneServer:
             gpu_s += ev0.elapsed_time(ev1) / 1e3
             ticks += 1
             for r in self.active:
-                r.remaining -= k
+                r.remaining = max(0, r.remaining - k)    # the device froze it at 0
             done = [r for r in self.active if r.remaining == 0]
             for r in done:
                 self.used -= footprint(r.spec)     # its memory is free for admissions

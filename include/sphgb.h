@@ -151,6 +151,19 @@ int sphgb_ctx_load_aos_f64(SphgbCtx* ctx, const double* d_pos_aos, const double*
 int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
                             double* d_rho, void* stream);
 
+/* Optional per-scene step limits: d_limits holds one int32 per scene on the
+ * device (NULL removes them).  A scene whose step counter (d_scene_step of
+ * sphgb_ctx_bind_state) has reached its limit is frozen: later steps leave its
+ * position, velocity, density, particle order and step counter unchanged
+ * (its particles still pass through the voxel hash).  One launch, or one
+ * captured graph, can so advance each scene of a batch by its own number of
+ * steps.  The array is read on the device at every step, so new values need
+ * no new call; a different pointer drops the context's captured graphs.
+ * Reconfiguring the context removes the limits.  No counterpart in the
+ * reference, which advances one scene per strategy object
+ * (state_generator.py:21-23). */
+int sphgb_ctx_set_step_limits(SphgbCtx* ctx, const int32_t* d_limits);
+
 /* Advance every scene n_steps steps (compute_next_state, repeated) on the
  * bound state.  With use_graph != 0 the n_steps sequence is captured once
  * into a CUDA graph and replayed on later calls with the same n_steps. */
