@@ -1350,6 +1350,19 @@ int sphgb_ctx_step_neighbours(SphgbCtx* ctx, int32_t* d_list, int32_t* d_count, 
 
 int sphgb_ctx_set_step_limits(SphgbCtx* ctx, const int32_t* d_limits) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
+    if (d_limits) {
+        // the kernels read it at every step: a host pointer would fault there
+        cudaPointerAttributes a{};
+        const cudaError_t e = cudaPointerGetAttributes(&a, d_limits);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SPHGB_ERR_INVALID, "d_limits is not a device pointer");
+        }
+        if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+            return fail(SPHGB_ERR_INVALID, "d_limits is not device or managed memory");
+        if ((reinterpret_cast<uintptr_t>(d_limits) & 3u) != 0)
+            return fail(SPHGB_ERR_INVALID, "d_limits is not 4-byte aligned");
+    }
     if (d_limits != ctx->step_limit) {
         // captured step graphs hold the old pointer
         for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);

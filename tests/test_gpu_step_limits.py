@@ -105,4 +105,10 @@ def test_removing_the_limits_and_reconfiguring():
     assert b.steps.cpu().tolist() == [2, 2]
     with pytest.raises(ValueError):
         b.set_step_limits([1, 2, 3])
+    # a host array is refused before any step could read it on the device
+    import ctypes as C
+    from sphgb import _capi
+    host = (C.c_int32 * 2)(1, 1)
+    assert _capi.load().sphgb_ctx_set_step_limits(b.handle, C.addressof(host)) == -1
+    assert "device" in _capi.last_error()
     b.close()
