@@ -506,9 +506,28 @@ struct Acc {
     }
 };
 
+// Two of those sums in one register pair, with sm_100's packed FP32 adds:
+// each element is rounded exactly as the scalar add rounds it, so the x and
+// y components give the scalar Acc's bits with half the add instructions.
+template <bool kPlain>
+struct Acc2 {
+    float2 s = make_float2(0.0f, 0.0f), c = make_float2(0.0f, 0.0f);
+    __device__ __forceinline__ void add(float2 x) {
+        if (kPlain) {
+            s = __fadd2_rn(s, x);
+        } else {
+            const float2 y = __fadd2_rn(x, make_float2(-c.x, -c.y));
+            const float2 t = __fadd2_rn(s, y);
+            c = __fadd2_rn(__fadd2_rn(t, make_float2(-s.x, -s.y)), make_float2(-y.x, -y.y));
+            s = t;
+        }
+    }
+};
+
 template <bool kPlain>
 struct ForceSums {
-    Acc<kPlain> px, py, pz, vx, vy, vz;
+    Acc2<kPlain> pxy, vxy;     // x and y components, packed
+    Acc<kPlain> pz, vz;
     int terms = 0;      // neighbours other than self
     bool bad = false;   // a neighbour factor was non-finite
 };
@@ -523,19 +542,18 @@ struct ForceSums {
 template <bool kPlain>
 __device__ __forceinline__ void add_pair(ForceSums<kPlain>& f, const float4& vi, float a_i,
                                          float inv_h, float gw, float lw, const float2& aj,
-                                         const float4& vj, float dx, float dy, float dz, float d2) {
+                                         const float4& vj, float2 dxy, float dz, float d2) {
     ++f.terms;
     if (!kPlain) f.bad |= !(fabsf(aj.x * aj.y) < INFINITY);
     const float r = sqrtf(d2);
     const float inv_r = 1.0f / r;
     const float t = __fmaf_rn(-r, inv_h, 1.0f);
     const float g = ((a_i + aj.x) * gw) * (t * t) * inv_r;
-    f.px.add(g * dx);
-    f.py.add(g * dy);
+    f.pxy.add(__fmul2_rn(make_float2(g, g), dxy));
     f.pz.add(g * dz);
     const float l = (lw * t) * aj.y;
-    f.vx.add(l * (vj.x - vi.x));
-    f.vy.add(l * (vj.y - vi.y));
+    const float2 dv = __fadd2_rn(make_float2(vj.x, vj.y), make_float2(-vi.x, -vi.y));
+    f.vxy.add(__fmul2_rn(make_float2(l, l), dv));
     f.vz.add(l * (vj.z - vi.z));
 }
 
@@ -553,7 +571,7 @@ __device__ __forceinline__ void force_sums(int s, const float4& pi, const float4
         if (j == s) return;
         float4 a, b;
         ldg256(fin + 2 * j, a, b);
-        add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(a.w, b.w), b, dx, dy, dz, d2);
+        add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(a.w, b.w), b, make_float2(dx, dy), dz, d2);
     });
 }
 
@@ -585,14 +603,12 @@ __device__ __forceinline__ void force_sums_list(const float4& pi, const float4& 
                 if (k0 + u0 + e >= cnt) break;
                 const float4& pj = pq[e];
                 const float4& vj = vq[e];
-                const float dx = __fsub_rn(pi.x, pj.x);
-                const float dy = __fsub_rn(pi.y, pj.y);
+                const float2 dxy = __fadd2_rn(make_float2(pi.x, pi.y), make_float2(-pj.x, -pj.y));
                 const float dz = __fsub_rn(pi.z, pj.z);
-                float d2 = __fmul_rn(dx, dx);
-                d2 = __fmaf_rn(dy, dy, d2);
+                float d2 = __fmul_rn(dxy.x, dxy.x);
+                d2 = __fmaf_rn(dxy.y, dxy.y, d2);
                 d2 = __fmaf_rn(dz, dz, d2);
-                add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(pj.w, vj.w), vj, dx, dy, dz,
-                         d2);
+                add_pair(f, vi, a_i, inv_h, gw, lw, make_float2(pj.w, vj.w), vj, dxy, dz, d2);
             }
         }
     }
@@ -619,14 +635,14 @@ __device__ __forceinline__ Forces forces_of(int s, const float4& pi, const float
         ForceSums<false> f;
         if (cnt >= 0) force_sums_list<false>(pi, vi, ai.x, sc, fin, list, n, cnt, f);
         else force_sums<false>(s, pi, vi, ai.x, sc, load_geom(sc), pos, fin, vstart, vcount, f);
-        out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
+        out = Forces{{f.pxy.s.x, f.pxy.s.y, f.pz.s}, {f.vxy.s.x, f.vxy.s.y, f.vz.s}, f.terms};
         plain = f.bad;
     }
     if (plain) {
         ForceSums<true> f;
         if (cnt >= 0) force_sums_list<true>(pi, vi, ai.x, sc, fin, list, n, cnt, f);
         else force_sums<true>(s, pi, vi, ai.x, sc, load_geom(sc), pos, fin, vstart, vcount, f);
-        out = Forces{{f.px.s, f.py.s, f.pz.s}, {f.vx.s, f.vy.s, f.vz.s}, f.terms};
+        out = Forces{{f.pxy.s.x, f.pxy.s.y, f.pz.s}, {f.vxy.s.x, f.vxy.s.y, f.vz.s}, f.terms};
     }
     return out;
 }
@@ -756,7 +772,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                 rare.idx[rare.base + atomicAdd(rare.count, 1)] = kRange ? row : s;
                 return;
             }
-            f = Forces{{fs.px.s, fs.py.s, fs.pz.s}, {fs.vx.s, fs.vy.s, fs.vz.s}, fs.terms};
+            f = Forces{{fs.pxy.s.x, fs.pxy.s.y, fs.pz.s}, {fs.vxy.s.x, fs.vxy.s.y, fs.vz.s}, fs.terms};
         } else {
             f = forces_of(s, pi, vi, ai, sc, pos, fin, vstart, vcount, list, n, cnt);
         }
