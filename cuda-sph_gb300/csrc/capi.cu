@@ -83,6 +83,9 @@ struct ConsChunk {
 constexpr int64_t kMaxParticles = SPHGB_MAX_PARTICLES;
 constexpr double kTileMaxOccupancy = 8.0;   // particles per voxel, table mean
 constexpr int kHostRanges = 8;
+// the pipelined host order: ranges of the force pass and buckets of the
+// density pass (host_step_pipelined)
+constexpr int kPipeRanges = 16;
 constexpr int kHostFirstRangeEvent = 6;
 // the host entry uploads the positions in kHostPosChunks parts; each is
 // converted and hashed while the next one is in flight
@@ -92,7 +95,7 @@ constexpr int kHostOrganizedEvent = kHostFirstChunkEvent + kHostPosChunks;
 constexpr int kHostEvents = kHostOrganizedEvent + 1;
 // device counters in big_count: big voxels, density tasks, tasks taken, then the
 // deferred particles of the whole force pass and of each host-entry range
-constexpr int kCounters = 4 + kHostRanges;
+constexpr int kCounters = 4 + (kHostRanges > kPipeRanges ? kHostRanges : kPipeRanges);
 
 struct SphgbCtx {
     int device = 0;
@@ -184,7 +187,20 @@ struct SphgbCtx {
     // force-pass order of the host-buffer entry point (sphgb_ctx_set_host_order)
     int host_order = SPHGB_HOST_ORDER_AUTO;
     int host_calls = 0;         // calls since the order was last set
-    double host_ms[3] = {};     // timed call per order (index = order)
+    double host_ms[4] = {};     // timed call per order (index = order)
+    // pipelined order (host_step_pipelined), allocated on its first call:
+    // density tasks bucketed by the original-index range of their first
+    // particle and the slots of each bucket's tasks, the latest bucket each
+    // voxel's tasks fall in, the counters, offsets and dependencies (on the
+    // device and page-locked), two more streams and their events
+    int2* tasks_b = nullptr;
+    int32_t* slots_b = nullptr;
+    int32_t* vbucket = nullptr;
+    int32_t* pipe_i = nullptr;
+    int32_t* h_pipe = nullptr;
+    size_t cap_tasks_b = 0, cap_vbucket = 0;
+    cudaStream_t host_stream3 = nullptr, host_stream4 = nullptr, host_stream5 = nullptr;
+    cudaEvent_t pipe_ev[3 + 2 * kPipeRanges] = {};
     std::map<int, cudaGraphExec_t> graphs;
 
     Launch launch(cudaStream_t st, bool ref_layout = false) const {
@@ -235,6 +251,16 @@ void free_ctx(SphgbCtx* c) {
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->host_stream) cudaStreamDestroy(c->host_stream);
     if (c->host_stream2) cudaStreamDestroy(c->host_stream2);
+    if (c->host_stream3) cudaStreamDestroy(c->host_stream3);
+    if (c->host_stream4) cudaStreamDestroy(c->host_stream4);
+    if (c->host_stream5) cudaStreamDestroy(c->host_stream5);
+    for (cudaEvent_t e : c->pipe_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->tasks_b) cudaFree(c->tasks_b);
+    if (c->slots_b) cudaFree(c->slots_b);
+    if (c->vbucket) cudaFree(c->vbucket);
+    if (c->pipe_i) cudaFree(c->pipe_i);
+    if (c->h_pipe) cudaFreeHost(c->h_pipe);
     for (cudaEvent_t e : c->host_ev)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -373,12 +399,12 @@ __global__ void k_slot_of(const int32_t* __restrict__ pbegin, int n_scenes, int 
 // state in original particle order as FP64 AoS: one thread per output row,
 // so the writes are coalesced (they may go to mapped host memory)
 __global__ void k_store_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
-                            int n_scenes, int n, const float4* __restrict__ pos,
+                            int n_scenes, int i0, int n, const float4* __restrict__ pos,
                             const float4* __restrict__ vel, const float* __restrict__ rho,
                             const int32_t* __restrict__ slot_of, const double* __restrict__ pos64,
                             double* __restrict__ pos_out, double* __restrict__ vel_out,
                             double* __restrict__ rho_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int si = scene_of(i, pbegin, n_scenes);
     const int s = __ldg(slot_of + i);
@@ -690,7 +716,7 @@ int enqueue_forces(SphgbCtx* c, const Launch& L, const PidRange* range, int rang
     RareList rare;
     rare.idx = c->rare;
     rare.count = c->big_count + 3 + (range ? 1 + range_index : 0);
-    rare.base = range ? range->i0 : 0;
+    rare.base = !range ? 0 : range->slots ? (int)(range->slots - c->slots_b) : range->i0;
     if (range)
         SPHGB_CUDA(launch_integrate_range(L, c->posB, c->velB, c->rho, c->fin, c->pidB, p64B,
                                           c->vstart, c->vcount, c->scene_step, c->nbr, pos_o,
@@ -875,6 +901,9 @@ int configure(SphgbCtx* c, const SphgbSceneParams* scenes, int n_scenes,
     c->bound = false;
     c->nbr_valid = false;
     c->step_limit = nullptr;   // one entry per scene of the old layout
+    // the host-entry orders are timed again on the new scenes
+    c->host_calls = 0;
+    c->host_ms[1] = c->host_ms[2] = c->host_ms[3] = 0.0;
     c->posA = c->velA = nullptr;
     c->rho = nullptr;
     c->pidA = nullptr;
@@ -1043,7 +1072,7 @@ int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
     k_slot_of<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                                  sep ? ctx->out_pid : ctx->pidA, ctx->slot_of);
     k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(
-        ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sep ? ctx->out_pos : ctx->posA,
+        ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n, sep ? ctx->out_pos : ctx->posA,
         sep ? ctx->out_vel : ctx->velA, ctx->rho, ctx->slot_of,
         sep ? ctx->out_pos64 : ctx->pos64A, d_pos_aos, d_vel_aos, d_rho);
     SPHGB_CUDA(cudaGetLastError());
@@ -1115,15 +1144,386 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
 }
 
 namespace {
+// ---- pipelined host entry ---------------------------------------------------
+// The density pass runs in kPipeK buckets of tasks, bucket b holding the
+// tasks whose first particle falls in range b of the original indices; the
+// force pass runs bucket by bucket over the same slots, in slot order, and
+// writes each particle's FP64 rows by its id.  A voxel's slots are in id
+// order, so a task's first particle has its smallest id and a particle of
+// range r is in a task of bucket r or earlier; only the overflow entry
+// (non-finite positions, arrival order) can put it in a later one.  Range r's
+// rows are complete, and download, once force buckets 0..max(r, dl[r]) are
+// done, dl[r] being the latest bucket of an overflow task holding a particle
+// of range r.  Force bucket b needs the densities and force
+// records of every neighbour of its particles, all of which lie in the 27
+// walk voxels around their voxels: dep[b] is the latest bucket of any task in
+// those voxels, and force bucket b starts as soon as density buckets
+// 0..dep[b] and their velocity gathers are done, while later buckets are
+// still in the density pass.  When particle ids follow space (a lattice in
+// index order), dep[b] is about b + 1 and the downloads overlap most of the
+// density pass; when they do not, dep[b] is the last bucket and the downloads
+// wait for the whole density pass.
+// pipe_i layout (kPipeK entries each): task counts per bucket, task fill
+// counters, task counters of the density launches, dep, task offsets, slot
+// counts, slot fill counters, slot offsets, dl.
+constexpr int kPipeK = kPipeRanges;
+constexpr int kPipeInts = 9 * kPipeK;
+
+__device__ __forceinline__ int range_of(int i, int n) {
+    int r = 0;
+    while (r + 1 < kPipeK && i >= (int)(((int64_t)n * (r + 1)) / kPipeK)) ++r;
+    return r;
+}
+
+// slots of a task: a run of at most kTaskRun from its first slot, within its voxel
+__device__ __forceinline__ int task_size(int2 t, const int32_t* __restrict__ vstart,
+                                         const int32_t* __restrict__ vcount) {
+    return min(kTaskRun, __ldg(vstart + t.x) + __ldg(vcount + t.x) - t.y);
+}
+
+// The bucket kernels aggregate per block in shared memory: one global atomic
+// per bucket and block, not one per task on kPipeK shared addresses.
+__global__ void k_bucket_count(const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
+                               const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
+                               const int32_t* __restrict__ vcount, int n,
+                               int32_t* __restrict__ pi) {
+    __shared__ int h[kPipeK], hs[kPipeK];
+    if (threadIdx.x < kPipeK) h[threadIdx.x] = hs[threadIdx.x] = 0;
+    __syncthreads();
+    const int m = *task_count;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const int2 t = tasks[k];
+        const int b = range_of(pid[t.y], n);
+        atomicAdd(h + b, 1);
+        atomicAdd(hs + b, task_size(t, vstart, vcount));
+    }
+    __syncthreads();
+    if (threadIdx.x < kPipeK && h[threadIdx.x]) {
+        atomicAdd(pi + threadIdx.x, h[threadIdx.x]);
+        atomicAdd(pi + 5 * kPipeK + threadIdx.x, hs[threadIdx.x]);
+    }
+}
+
+// Each block places a block-sized run of tasks per round, so a bucket keeps
+// the tasks' voxel order up to the order in which blocks take their places.
+__global__ void k_bucket_scatter(const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
+                                 const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
+                                 const int32_t* __restrict__ vcount, int n, int32_t* __restrict__ pi,
+                                 int2* __restrict__ tasks_b, int32_t* __restrict__ slots_b,
+                                 int32_t* __restrict__ vbucket) {
+    __shared__ int cnt[kPipeK], scnt[kPipeK], base[kPipeK], sbase[kPipeK];
+    int off[kPipeK], soff[kPipeK];
+    int acc = 0, sacc = 0;
+    for (int b = 0; b < kPipeK; ++b) {
+        off[b] = acc;
+        soff[b] = sacc;
+        acc += pi[b];
+        sacc += pi[5 * kPipeK + b];
+    }
+    if (blockIdx.x == 0 && threadIdx.x < kPipeK) {
+        pi[4 * kPipeK + threadIdx.x] = off[threadIdx.x];
+        pi[7 * kPipeK + threadIdx.x] = soff[threadIdx.x];
+    }
+    const int m = *task_count;
+    for (int k0 = blockIdx.x * blockDim.x; k0 < m; k0 += gridDim.x * blockDim.x) {
+        const int k = k0 + threadIdx.x;
+        if (threadIdx.x < kPipeK) cnt[threadIdx.x] = scnt[threadIdx.x] = 0;
+        __syncthreads();
+        int2 t = make_int2(0, 0);
+        int b = -1, local = 0, slocal = 0, sz = 0;
+        if (k < m) {
+            t = tasks[k];
+            b = range_of(pid[t.y], n);
+            sz = task_size(t, vstart, vcount);
+            local = atomicAdd(cnt + b, 1);
+            slocal = atomicAdd(scnt + b, sz);
+        }
+        __syncthreads();
+        if (threadIdx.x < kPipeK && cnt[threadIdx.x]) {
+            base[threadIdx.x] = atomicAdd(pi + kPipeK + threadIdx.x, cnt[threadIdx.x]);
+            sbase[threadIdx.x] = atomicAdd(pi + 6 * kPipeK + threadIdx.x, scnt[threadIdx.x]);
+        }
+        __syncthreads();
+        if (b >= 0) {
+            tasks_b[off[b] + base[b] + local] = t;
+            int32_t* dst = slots_b + soff[b] + sbase[b] + slocal;
+            for (int j = 0; j < sz; ++j) dst[j] = t.y + j;
+            atomicMax(vbucket + t.x, b);
+        }
+        __syncthreads();
+    }
+}
+
+// dep[b] = max over the tasks of bucket b of the latest bucket in the task
+// voxel's 27 walk voxels (one scene, walk dims = table dims); dl[r] = max
+// bucket of an overflow task holding a particle of range r
+__global__ void k_bucket_deps(const SceneDev* __restrict__ scenes, const int2* __restrict__ tasks,
+                              const int32_t* __restrict__ task_count,
+                              const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
+                              const int32_t* __restrict__ vcount,
+                              const int32_t* __restrict__ vbucket, int n,
+                              int32_t* __restrict__ pi) {
+    __shared__ int dep[kPipeK], dl[kPipeK];
+    if (threadIdx.x < kPipeK) dep[threadIdx.x] = dl[threadIdx.x] = -1;
+    __syncthreads();
+    const SceneDev& sc = scenes[0];
+    const int m = *task_count;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const int2 t = tasks[k];
+        const int vid = t.x;
+        const int b = range_of(pid[t.y], n);
+        int need = vbucket[vid];
+        const int local = vid - sc.v_begin;
+        if (local == sc.v_count) {      // the overflow entry: no neighbours, ids unordered
+            const int end = t.y + task_size(t, vstart, vcount);
+            for (int d = t.y; d < end; ++d) atomicMax(dl + range_of(pid[d], n), b);
+        } else {
+            const Udiv q0{sc.div_m[0], sc.div_s[0]}, q1{sc.div_m[1], sc.div_s[1]};
+            int vx, vy, vz;
+            if (sc.tiled) {
+                const int tl = local >> 6, in = local & 63;
+                const int r0 = q0.div(tl), r1 = q1.div(r0);
+                vx = ((tl - r0 * sc.nt0) << 2) | (in & 3);
+                vy = ((r0 - r1 * sc.nt1) << 2) | ((in >> 2) & 3);
+                vz = (r1 << 2) | (in >> 4);
+            } else {
+                const int r0 = q0.div(local), r1 = q1.div(r0);
+                vx = local - r0 * sc.dims[0];
+                vy = r0 - r1 * sc.dims[1];
+                vz = r1;
+            }
+            for (int w = 0; w < 27; ++w) {
+                const int nx = vx + w / 9 - 1, ny = vy + (w / 3) % 3 - 1, nz = vz + w % 3 - 1;
+                if (nx < 0 || nx >= sc.wdims[0] || ny < 0 || ny >= sc.wdims[1] || nz < 0 ||
+                    nz >= sc.wdims[2])
+                    continue;
+                const int u = sc.v_begin + voxel_index(nx, ny, nz, sc.tiled, sc.wdims[0],
+                                                       sc.wdims[1], sc.nt0, sc.nt1);
+                need = max(need, vbucket[u]);
+            }
+        }
+        atomicMax(dep + b, need);
+    }
+    __syncthreads();
+    if (threadIdx.x < kPipeK && dep[threadIdx.x] >= 0)
+        atomicMax(pi + 3 * kPipeK + threadIdx.x, dep[threadIdx.x]);
+    if (threadIdx.x < kPipeK && dl[threadIdx.x] >= 0)
+        atomicMax(pi + 8 * kPipeK + threadIdx.x, dl[threadIdx.x]);
+}
+
+// One scene with a neighbour list the warp kernel builds, enough particles
+// for the buckets, and no step limits (a frozen scene has no density tasks,
+// and the force pass runs only the tasks' slots).
+bool pipelined_eligible(const SphgbCtx* c) {
+    return c->n_scenes == 1 && !c->h_scenes[0].walk_trunc && c->h_scenes[0].cap <= kListCap &&
+           c->density_variant == SPHGB_DENSITY_WARP && c->n >= 32 * kPipeK && !c->step_limit;
+}
+
+int ensure_pipelined(SphgbCtx* c) {
+    const size_t N = (size_t)c->n, V = (size_t)c->v_total;
+    if (c->cap_tasks_b < N) {
+        if (c->tasks_b) cudaFree(c->tasks_b);
+        if (c->slots_b) cudaFree(c->slots_b);
+        c->tasks_b = nullptr;
+        c->slots_b = nullptr;
+        c->cap_tasks_b = 0;
+        int rc = dalloc(&c->tasks_b, N);
+        if (!rc) rc = dalloc(&c->slots_b, N);
+        if (rc) return rc;
+        c->cap_tasks_b = N;
+    }
+    if (c->cap_vbucket < V) {
+        if (c->vbucket) cudaFree(c->vbucket);
+        c->vbucket = nullptr;
+        c->cap_vbucket = 0;
+        int rc = dalloc(&c->vbucket, V);
+        if (rc) return rc;
+        c->cap_vbucket = V;
+    }
+    if (!c->pipe_i) {
+        int rc = dalloc(&c->pipe_i, (size_t)kPipeInts);
+        if (rc) return rc;
+    }
+    if (!c->h_pipe) SPHGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&c->h_pipe),
+                                             sizeof(int32_t) * kPipeInts, cudaHostAllocDefault));
+    if (!c->host_stream3) {
+        // the gathers and force buckets go ahead of the density buckets when
+        // both have blocks waiting for an SM
+        int least = 0, greatest = 0;
+        SPHGB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SPHGB_CUDA(cudaStreamCreateWithPriority(&c->host_stream3, cudaStreamNonBlocking, greatest));
+    }
+    if (!c->host_stream4)
+        SPHGB_CUDA(cudaStreamCreateWithFlags(&c->host_stream4, cudaStreamNonBlocking));
+    if (!c->host_stream5)
+        SPHGB_CUDA(cudaStreamCreateWithFlags(&c->host_stream5, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : c->pipe_ev)
+        if (!e) SPHGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return SPHGB_OK;
+}
+
+// The host entry after the positions have been hashed (st) and the
+// velocities uploaded (st2, event e_vel): the step with its force pass and
+// downloads pipelined behind the density pass (see kPipeK above).  st sorts,
+// buckets the tasks and runs the density buckets; st3, which has the
+// greatest priority, builds the slot map, gathers each bucket's velocities
+// and runs the force buckets, each after the gathers of the buckets it
+// depends on; st4 reads the counts and dependencies back and downloads each
+// range's rows.
+int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, double* sr,
+                        double* h_pos_out, double* h_vel_out, double* h_rho_out) {
+    const size_t N = (size_t)c->n;
+    cudaStream_t st = c->host_stream, st3 = c->host_stream3, st4 = c->host_stream4,
+                 st5 = c->host_stream5;
+    cudaEvent_t e_org = c->pipe_ev[0], e_bk = c->pipe_ev[1], e_dep = c->pipe_ev[2];
+    cudaEvent_t* e_bucket = c->pipe_ev + 3;
+    cudaEvent_t* e_range = c->pipe_ev + 3 + kPipeK;
+    const Launch L = c->launch(st);
+    const Launch L3 = c->launch(st3);
+    double* p64A = c->any_pipe ? c->pos64A : nullptr;
+    double* p64B = c->any_pipe ? c->pos64B : nullptr;
+    // sort (the velocities follow after the density pass, per bucket)
+    int rc = enqueue_organize(c, L, c->posA, nullptr, c->pidA, p64A, c->posB, c->velB, c->pidB,
+                              p64B, c->vstart, c->vcount, nullptr, true, true);
+    if (rc) return rc;
+    SPHGB_CUDA(cudaEventRecord(e_org, st));
+    // st3: original index -> slot (the deferred particles of the force pass
+    // are listed by row), then the velocity upload; the gathers read its FP64
+    // rows, and a force bucket overwrites only the rows of its own
+    // particles, which its gathers have read
+    SPHGB_CUDA(cudaStreamWaitEvent(st3, e_org, 0));
+    k_slot_of<<<blocks(c->n), kBlock, 0, st3>>>(c->d_pbegin, c->n_scenes, c->n, c->pidB,
+                                                 c->slot_of);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaStreamWaitEvent(st3, e_vel, 0));
+    // buckets and dependencies
+    int32_t* pi = c->pipe_i;
+    const int32_t* n_tasks = c->big_count + 1;
+    const int grid = device_sm_count() * 4;
+    SPHGB_CUDA(cudaMemsetAsync(pi, 0, sizeof(int32_t) * kPipeInts, st));
+    SPHGB_CUDA(cudaMemsetAsync(c->vbucket, 0xff, sizeof(int32_t) * c->v_total, st));
+    k_bucket_count<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount,
+                                            c->n, pi);
+    k_bucket_scatter<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount,
+                                              c->n, pi, c->tasks_b, c->slots_b, c->vbucket);
+    k_bucket_deps<<<grid, kBlock, 0, st>>>(c->d_scenes, c->tasks_b, n_tasks, c->pidB, c->vstart,
+                                           c->vcount, c->vbucket, c->n, pi);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaEventRecord(e_bk, st));
+    SPHGB_CUDA(cudaStreamWaitEvent(st4, e_bk, 0));
+    SPHGB_CUDA(cudaMemcpyAsync(c->h_pipe, pi, sizeof(int32_t) * kPipeInts,
+                               cudaMemcpyDeviceToHost, st4));
+    SPHGB_CUDA(cudaEventRecord(e_dep, st4));
+    // the density buckets are independent of one another: they alternate
+    // between st and st5, so that one bucket's last tasks overlap the next
+    // bucket's first
+    SPHGB_CUDA(cudaStreamWaitEvent(st5, e_bk, 0));
+    const Launch L5 = c->launch(st5);
+    for (int b = 0; b < kPipeK; ++b) {
+        SPHGB_CUDA(launch_density_wc(b % 2 ? L5 : L, c->posB, nullptr, c->vstart, c->vcount,
+                                     c->rho, c->fin, c->nbr, c->tasks_b, pi + b,
+                                     pi + 2 * kPipeK + b, pi + 4 * kPipeK + b));
+        SPHGB_CUDA(cudaEventRecord(e_bucket[b], b % 2 ? st5 : st));
+    }
+    c->nbr_valid = true;
+    // the slot counts and dependencies are needed on the host to launch and
+    // order the force buckets
+    SPHGB_CUDA(cudaEventSynchronize(e_dep));
+    const int32_t* h_dep = c->h_pipe + 3 * kPipeK;
+    const int32_t* h_slots = c->h_pipe + 5 * kPipeK;
+    const int32_t* h_soff = c->h_pipe + 7 * kPipeK;
+    const int32_t* h_dl = c->h_pipe + 8 * kPipeK;
+    int gathered = 0;   // buckets whose velocities are gathered on st3
+    auto gather_through = [&](int last) -> int {
+        for (; gathered <= last; ++gathered) {
+            SPHGB_CUDA(cudaStreamWaitEvent(st3, e_bucket[gathered], 0));
+            SPHGB_CUDA(launch_gather_vel_tasks(L3, c->pidB, c->tasks_b, pi + gathered,
+                                               pi + 4 * kPipeK + gathered, c->vstart, c->vcount,
+                                               sv, c->rho, c->velB, c->fin));
+        }
+        return SPHGB_OK;
+    };
+    // range r is stored in original order (FP64 rows, on st3) and downloaded
+    // once force bucket max(r, dl[r]) is done; a range's store overwrites
+    // the uploaded velocity rows of its particles, which their buckets'
+    // gathers, all at or before that force bucket, have read
+    const bool sep = c->out_pos != nullptr;
+    int next_r = 0;
+    auto download_through = [&](int b) -> int {
+        for (; next_r < kPipeK && std::max(next_r, (int)h_dl[next_r]) <= b; ++next_r) {
+            const size_t i0 = N * next_r / kPipeK, i1 = N * (next_r + 1) / kPipeK;
+            if (i1 > i0)
+                k_store_aos<<<blocks((int)(i1 - i0)), kBlock, 0, st3>>>(
+                    c->d_scenes, c->d_pbegin, c->n_scenes, (int)i0, (int)i1,
+                    sep ? c->out_pos : c->posA, sep ? c->out_vel : c->velA, c->rho, c->slot_of,
+                    c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr, sp, sv, sr);
+            SPHGB_CUDA(cudaGetLastError());
+            SPHGB_CUDA(cudaEventRecord(e_range[next_r], st3));
+            SPHGB_CUDA(cudaStreamWaitEvent(st4, e_range[next_r], 0));
+            SPHGB_CUDA(cudaMemcpyAsync(h_pos_out + 3 * i0, sp + 3 * i0,
+                                       sizeof(double) * 3 * (i1 - i0), cudaMemcpyDeviceToHost,
+                                       st4));
+            SPHGB_CUDA(cudaMemcpyAsync(h_vel_out + 3 * i0, sv + 3 * i0,
+                                       sizeof(double) * 3 * (i1 - i0), cudaMemcpyDeviceToHost,
+                                       st4));
+            SPHGB_CUDA(cudaMemcpyAsync(h_rho_out + i0, sr + i0, sizeof(double) * (i1 - i0),
+                                       cudaMemcpyDeviceToHost, st4));
+        }
+        return SPHGB_OK;
+    };
+    size_t listed = 0;
+    for (int b = 0; b < kPipeK; ++b) {
+        rc = gather_through(std::min(std::max(h_dep[b], b), kPipeK - 1));
+        if (rc) return rc;
+        if (h_slots[b] < 0 || h_soff[b] < 0 || (size_t)h_soff[b] + h_slots[b] > N)
+            return fail(SPHGB_ERR_STATE, "pipelined step: bucket slot counts out of range");
+        listed += (size_t)h_slots[b];
+        PidRange range;
+        range.slots = c->slots_b + h_soff[b];
+        range.n_slots = h_slots[b];
+        rc = enqueue_forces(c, L3, &range, b);
+        if (rc) return rc;
+        rc = download_through(b);
+        if (rc) return rc;
+    }
+    if (next_r != kPipeK) return fail(SPHGB_ERR_STATE, "pipelined step: range left undownloaded");
+    // every bucket gathered (the slot-order velocities are complete), then
+    // the checks and the step counter
+    rc = gather_through(kPipeK - 1);
+    if (rc) return rc;
+    rc = enqueue_checks(c, st3);
+    if (rc) return rc;
+    k_step_counter<<<blocks(c->n_scenes, 128), 128, 0, st3>>>(c->scene_step, c->n_scenes,
+                                                                c->step_limit);
+    SPHGB_CUDA(cudaGetLastError());
+    SPHGB_CUDA(cudaStreamSynchronize(st4));
+    SPHGB_CUDA(cudaStreamSynchronize(st3));
+    SPHGB_CUDA(cudaStreamSynchronize(st5));
+    SPHGB_CUDA(cudaStreamSynchronize(st));
+    // every slot was in exactly one bucket
+    if (listed != N) return fail(SPHGB_ERR_STATE, "pipelined step: buckets missed particles");
+    return SPHGB_OK;
+}
+
 // Force-pass order of the next host-entry call.  AUTO: call 1 (allocations,
-// first touches) and call 2 run in slot order, call 3 in particle order; calls 2
-// and 3 are timed, and later calls take the faster order.
+// first touches) and call 2 run in slot order, call 3 in particle order and
+// call 4 pipelined (when the context allows it); calls 2 to 4 are timed, and
+// later calls take the fastest order the context allows.
 int host_order_for_call(const SphgbCtx* c) {
-    if (c->host_order != SPHGB_HOST_ORDER_AUTO) return c->host_order;
+    const bool pipe_ok = pipelined_eligible(c);
+    if (c->host_order != SPHGB_HOST_ORDER_AUTO) {
+        if (c->host_order == SPHGB_HOST_ORDER_PIPELINED && !pipe_ok) return SPHGB_HOST_ORDER_PARTICLE;
+        return c->host_order;
+    }
     if (c->host_calls < 2) return SPHGB_HOST_ORDER_SLOT;
     if (c->host_calls == 2) return SPHGB_HOST_ORDER_PARTICLE;
-    return c->host_ms[SPHGB_HOST_ORDER_PARTICLE] < c->host_ms[SPHGB_HOST_ORDER_SLOT]
-               ? SPHGB_HOST_ORDER_PARTICLE : SPHGB_HOST_ORDER_SLOT;
+    if (c->host_calls == 3 && pipe_ok) return SPHGB_HOST_ORDER_PIPELINED;
+    int best = SPHGB_HOST_ORDER_SLOT;
+    for (int o = SPHGB_HOST_ORDER_PARTICLE; o <= SPHGB_HOST_ORDER_PIPELINED; ++o)
+        if (c->host_ms[o] > 0.0 && c->host_ms[o] < c->host_ms[best] &&
+            (o != SPHGB_HOST_ORDER_PIPELINED || pipe_ok))
+            best = o;
+    return best;
 }
 }  // namespace
 
@@ -1212,13 +1612,32 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
             SPHGB_CUDA(launch_hash_count(L, ctx->posA, ctx->cell, ctx->slot, ctx->vcount, i0, i1));
         }
     }
-    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, b3, cudaMemcpyHostToDevice, st2));
-    k_load_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n,
-                                       nullptr, sv, ctx->posA, ctx->velA, ctx->pidA, nullptr);
-    SPHGB_CUDA(cudaGetLastError());
-    SPHGB_CUDA(cudaEventRecord(e_vel, st2));
     const int order = host_order_for_call(ctx);
+    SPHGB_CUDA(cudaMemcpyAsync(sv, h_vel, b3, cudaMemcpyHostToDevice, st2));
+    // the pipelined order gathers from the FP64 rows bucket by bucket
+    if (order != SPHGB_HOST_ORDER_PIPELINED) {
+        k_load_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n,
+                                           nullptr, sv, ctx->posA, ctx->velA, ctx->pidA, nullptr);
+        SPHGB_CUDA(cudaGetLastError());
+    }
+    SPHGB_CUDA(cudaEventRecord(e_vel, st2));
     const auto t0 = std::chrono::steady_clock::now();
+    auto record_time = [&]() {
+        const double ms = std::chrono::duration<double, std::milli>(
+                              std::chrono::steady_clock::now() - t0).count();
+        if (ctx->host_calls < 1000) ++ctx->host_calls;
+        // calls 2, 3 and 4 time the three orders (call 1 warms up)
+        if (ctx->host_order == SPHGB_HOST_ORDER_AUTO && ctx->host_calls >= 2 &&
+            ctx->host_calls <= 4)
+            ctx->host_ms[order] = ms;
+    };
+    if (order == SPHGB_HOST_ORDER_PIPELINED) {
+        int rc = ensure_pipelined(ctx);
+        if (!rc) rc = host_step_pipelined(ctx, e_vel, sp, sv, sr, h_pos_out, h_vel_out, h_rho_out);
+        if (rc) return rc;
+        record_time();
+        return SPHGB_OK;
+    }
     cudaEvent_t e_org = ctx->host_ev[kHostOrganizedEvent];
     int rc = enqueue_step(ctx, st, nullptr, e_vel, e_rho, order == SPHGB_HOST_ORDER_SLOT, true,
                           e_org);
@@ -1232,7 +1651,7 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_slot, st2));
     SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
-    k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+    k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n,
                                         nullptr, nullptr, ctx->rho, ctx->slot_of, nullptr,
                                         nullptr, nullptr, sr);
     SPHGB_CUDA(cudaGetLastError());
@@ -1243,8 +1662,8 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
         SPHGB_CUDA(cudaEventRecord(e_done, st2));
         SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
         const bool sep = ctx->out_pos != nullptr;
-        k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
-                                           sep ? ctx->out_pos : ctx->posA,
+        k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0,
+                                           ctx->n, sep ? ctx->out_pos : ctx->posA,
                                            sep ? ctx->out_vel : ctx->velA, nullptr, ctx->slot_of,
                                            sep ? ctx->out_pos64 : ctx->pos64A, sp, sv, nullptr);
         SPHGB_CUDA(cudaGetLastError());
@@ -1279,22 +1698,19 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
         SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
     }
     SPHGB_CUDA(cudaStreamSynchronize(st));
-    const double ms =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (ctx->host_calls < 1000) ++ctx->host_calls;
-    if (ctx->host_order == SPHGB_HOST_ORDER_AUTO && ctx->host_calls >= 2 && ctx->host_calls <= 3)
-        ctx->host_ms[order] = ms;   // calls 2 and 3 time the two orders (call 1 warms up)
+    record_time();
     return SPHGB_OK;
 }
 
 int sphgb_ctx_set_host_order(SphgbCtx* ctx, int order) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (order != SPHGB_HOST_ORDER_AUTO && order != SPHGB_HOST_ORDER_SLOT &&
-        order != SPHGB_HOST_ORDER_PARTICLE)
-        return fail(SPHGB_ERR_INVALID, "order must be SPHGB_HOST_ORDER_AUTO, _SLOT or _PARTICLE");
+        order != SPHGB_HOST_ORDER_PARTICLE && order != SPHGB_HOST_ORDER_PIPELINED)
+        return fail(SPHGB_ERR_INVALID,
+                    "order must be SPHGB_HOST_ORDER_AUTO, _SLOT, _PARTICLE or _PIPELINED");
     ctx->host_order = order;
     ctx->host_calls = 0;
-    ctx->host_ms[1] = ctx->host_ms[2] = 0.0;
+    ctx->host_ms[1] = ctx->host_ms[2] = ctx->host_ms[3] = 0.0;
     return SPHGB_OK;
 }
 

@@ -462,6 +462,10 @@ struct NbrList {
 struct PidRange {
     const int32_t* slot_of = nullptr;
     int i0 = 0, i1 = 0;
+    // list mode (slots set): the pass runs slots[0..n_slots) in that order
+    // instead and writes the slot-order state only (no FP64 rows)
+    const int32_t* slots = nullptr;
+    int n_slots = 0;
     double* pos = nullptr;      // (n, 3) FP64
     double* vel = nullptr;      // (n, 3) FP64
 };
@@ -539,10 +543,19 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel
                            float4* fin, NbrList nbr);
 // the step's density pass: one warp per task (<= kTaskRun particles of one voxel);
 // task_next: a zeroed counter from which the warps take the tasks
+// task_offset (optional, device): the tasks start at tasks[*task_offset] (one
+// bucket of a bucketed list)
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
-                              const int32_t* task_count, int32_t* task_next);
+                              const int32_t* task_count, int32_t* task_next,
+                              const int32_t* task_offset = nullptr);
+// k_gather_vel over the slots of a bucket of density tasks
+cudaError_t launch_gather_vel_tasks(const Launch& L, const int32_t* pid, const int2* tasks,
+                                    const int32_t* task_count, const int32_t* task_offset,
+                                    const int32_t* vstart, const int32_t* vcount,
+                                    const double* vel64, const float* rho, float4* vel_out,
+                                    float4* fin);
 cudaError_t launch_gather_vel(const Launch& L, const int32_t* pid, const float4* vel_in,
                               const float* rho, float4* vel_out, float4* fin);
 cudaError_t launch_forces(const Launch& L, const float4* pos, const float4* vel,

@@ -298,13 +298,14 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
              const int32_t* __restrict__ vcount, float* __restrict__ rho,
              float4* __restrict__ fin, NbrList nbr,
              const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
-             int32_t* __restrict__ task_next) {
+             int32_t* __restrict__ task_next, const int32_t* __restrict__ task_offset) {
     __shared__ WcShared sh[kWcWarps];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     WcShared& S = sh[threadIdx.x >> 5];
     const unsigned lt = (1u << lane) - 1u;
     const int n_tasks = *task_count;
+    if (task_offset) tasks += *task_offset;   // one bucket of a bucketed task list
     // Each warp takes its next task from a counter when it is done with the
     // last one: the cost of a task varies with its voxel's neighbourhood, and
     // a fixed share per warp left warps idle at the end of the pass (15 % of
@@ -474,6 +475,35 @@ k_gather_vel(const int32_t* __restrict__ pbegin, int n_scenes, int n,
     const float4 v = __ldg(vel_in + __ldg(pbegin + scene_of(d, pbegin, n_scenes)) + __ldg(pid + d));
     vel_out[d] = v;
     fin[2 * d + 1] = make_float4(v.x, v.y, v.z, 1.0f / __ldg(rho + d));
+}
+
+// The same for the slots of a bucket of density tasks (pipelined host
+// entry): one thread per slot of the bucket's tasks (a task's run of at most
+// kTaskRun slots of one voxel), kTaskRun threads per task.  The velocities
+// come straight from the uploaded FP64 rows (original order), converted as
+// k_load_aos converts them: the float4 state buffer is the force pass's
+// output, which earlier force buckets are already writing (in slot order)
+// while later buckets gather.
+__global__ void __launch_bounds__(kBlock)
+k_gather_vel_tasks(const int32_t* __restrict__ pbegin, int n_scenes, const int32_t* __restrict__ pid,
+                   const int32_t* __restrict__ vstart, const int32_t* __restrict__ vcount,
+                   const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
+                   const int32_t* __restrict__ task_offset, const double* __restrict__ vel64,
+                   const float* __restrict__ rho, float4* __restrict__ vel_out,
+                   float4* __restrict__ fin) {
+    const int64_t n_threads = (int64_t)*task_count * kTaskRun;
+    const int2* tk = tasks + *task_offset;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n_threads;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int2 task = tk[q / kTaskRun];
+        const int d = task.y + (int)(q % kTaskRun);
+        if (d >= __ldg(vstart + task.x) + __ldg(vcount + task.x)) continue;
+        const double* r =
+            vel64 + 3 * (size_t)(__ldg(pbegin + scene_of(d, pbegin, n_scenes)) + __ldg(pid + d));
+        const float4 v = make_float4((float)__ldg(r), (float)__ldg(r + 1), (float)__ldg(r + 2), 0.0f);
+        vel_out[d] = v;
+        fin[2 * d + 1] = make_float4(v.x, v.y, v.z, 1.0f / __ldg(rho + d));
+    }
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -688,14 +718,19 @@ k_forces(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin
 constexpr int kForceAll = 0, kForceLean = 1, kForceRare = 2;
 // kForceRare grid: one block per SM (device_sm_count())
 
+// Which particles a force launch runs: every slot (kBySlot); the particles of
+// rows range.i0..i1 in original order, which also write the FP64 rows of the
+// next position and velocity (kByRow); or the slots range.slots[0..n_slots)
+// (kByList), which write the slot-order state only, like kBySlot.
+constexpr int kBySlot = 0, kByRow = 1, kByList = 2;
+
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
 // (collision_kernel_box :75-98 or collision_kernel :56-72).  Writes the next
 // state into the *_out buffers at the same slot.  kPipe = false is the
-// instantiation for contexts without pipe scenes (no FP64 code).  kRange:
-// one thread per particle of range.i0..i1 in original order (same per-particle
-// arithmetic), which also writes the FP64 rows of the next position and
-// velocity.  kMode: see kForceAll.
-template <bool kPipe, bool kRange, int kMode>
+// instantiation for contexts without pipe scenes (no FP64 code).  kIdx: see
+// kBySlot; the per-particle arithmetic is the same in all three.  kMode: see
+// kForceAll.
+template <bool kPipe, int kIdx, int kMode>
 __global__ void __launch_bounds__(kBlock, 4)
 k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin, int n_scenes,
             int n, const double* __restrict__ pipe, const float4* __restrict__ pos,
@@ -711,12 +746,17 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     // particle per thread (the body runs once)
     const int m_rare = kMode == kForceRare ? *rare.count : 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
+        // deferred particles are listed by row (kByRow) or by slot
+        constexpr bool by_row = kIdx == kByRow;
         int s, row = 0;
         if (kMode == kForceRare) {
             if (k >= m_rare) return;
             row = rare.idx[rare.base + k];
-            s = kRange ? __ldg(range.slot_of + row) : row;
-        } else if (kRange) {
+            s = by_row ? __ldg(range.slot_of + row) : row;
+        } else if (kIdx == kByList) {
+            if (k >= range.n_slots) return;
+            s = __ldg(range.slots + k);
+        } else if (by_row) {
             row = range.i0 + k;
             if (row >= range.i1) return;
             s = __ldg(range.slot_of + row);
@@ -740,7 +780,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                     if (sc.mode == 1) x64[a] = pos64[3 * s + a];
                 }
             }
-            if (kRange) {
+            if (by_row) {
                 for (int a = 0; a < 3; ++a) range.pos[3 * (size_t)row + a] = x64[a];
                 range.vel[3 * (size_t)row + 0] = v4.x;
                 range.vel[3 * (size_t)row + 1] = v4.y;
@@ -769,7 +809,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                 ok = !fs.bad;
             }
             if (!ok) {
-                rare.idx[rare.base + atomicAdd(rare.count, 1)] = kRange ? row : s;
+                rare.idx[rare.base + atomicAdd(rare.count, 1)] = by_row ? row : s;
                 return;
             }
             f = Forces{{fs.pxy.s.x, fs.pxy.s.y, fs.pz.s}, {fs.vxy.s.x, fs.vxy.s.y, fs.vz.s}, fs.terms};
@@ -801,7 +841,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                 pos64_out[3 * s + 1] = x[1];
                 pos64_out[3 * s + 2] = x[2];
             }
-            if (kRange) {
+            if (by_row) {
                 range.pos[3 * (size_t)row + 0] = x[0];
                 range.pos[3 * (size_t)row + 1] = x[1];
                 range.pos[3 * (size_t)row + 2] = x[2];
@@ -820,12 +860,12 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             for (int a = 0; a < 3; ++a) {
                 v[a] = (float)vd[a];
                 pos64_out[3 * s + a] = x[a];
-                if (kRange) range.pos[3 * (size_t)row + a] = x[a];
+                if (by_row) range.pos[3 * (size_t)row + a] = x[a];
             }
             pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
         }
         vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
-        if (kRange) {
+        if (by_row) {
             range.vel[3 * (size_t)row + 0] = v[0];
             range.vel[3 * (size_t)row + 1] = v[1];
             range.vel[3 * (size_t)row + 2] = v[2];
@@ -875,7 +915,8 @@ cudaError_t launch_density(const Launch& L, const float4* pos, const float4* vel
 cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* vel,
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
-                              const int32_t* task_count, int32_t* task_next) {
+                              const int32_t* task_count, int32_t* task_next,
+                              const int32_t* task_offset) {
     if (L.n == 0) return cudaSuccess;
     // persistent grid: up to 4 blocks of 8 warps per SM, warps take tasks in turn
     int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
@@ -884,7 +925,7 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
     auto kernel = L.layout == 1 ? k_density_wc<1> : L.layout == 2 ? k_density_wc<2> : k_density_wc<0>;
     kernel<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
                                                    vstart, vcount, rho, fin, nbr, tasks, task_count,
-                                                   task_next);
+                                                   task_next, task_offset);
     return cudaGetLastError();
 }
 
@@ -893,6 +934,18 @@ cudaError_t launch_gather_vel(const Launch& L, const int32_t* pid, const float4*
     if (L.n == 0) return cudaSuccess;
     k_gather_vel<<<blocks_for(L.n), kBlock, 0, L.stream>>>(L.pbegin, L.n_scenes, L.n, pid, vel_in,
                                                             rho, vel_out, fin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_vel_tasks(const Launch& L, const int32_t* pid, const int2* tasks,
+                                    const int32_t* task_count, const int32_t* task_offset,
+                                    const int32_t* vstart, const int32_t* vcount,
+                                    const double* vel64, const float* rho, float4* vel_out,
+                                    float4* fin) {
+    if (L.n == 0) return cudaSuccess;
+    k_gather_vel_tasks<<<device_sm_count() * 4, kBlock, 0, L.stream>>>(
+        L.pbegin, L.n_scenes, pid, vstart, vcount, tasks, task_count, task_offset, vel64, rho,
+        vel_out, fin);
     return cudaGetLastError();
 }
 
@@ -919,7 +972,7 @@ namespace {
 // the force pass of one launch shape: with a neighbour list and a RareList
 // (contexts without pipe scenes), the lean pass then the deferred particles;
 // otherwise every particle in one pass
-template <bool kRange>
+template <int kIdx>
 cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const float4* vel,
                               const float* rho, const float4* fin, const int32_t* pid,
                               const double* pos64, const int32_t* vstart, const int32_t* vcount,
@@ -927,23 +980,23 @@ cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const f
                               float4* vel_out, int32_t* pid_out, double* pos64_out,
                               float4* force_out, PidRange range, RareList rare) {
     if (L.pipe_scenes) {
-        k_integrate<true, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<true, kIdx, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
             RareList{}, L.step_limit);
     } else if (nbr.count && rare.count) {
-        k_integrate<false, kRange, kForceLean><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<false, kIdx, kForceLean><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
             L.step_limit);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        k_integrate<false, kRange, kForceRare><<<device_sm_count(), kBlock, 0, L.stream>>>(
+        k_integrate<false, kIdx, kForceRare><<<device_sm_count(), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
             L.step_limit);
     } else {
-        k_integrate<false, kRange, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<false, kIdx, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
             RareList{}, L.step_limit);
@@ -959,7 +1012,7 @@ cudaError_t launch_integrate(const Launch& L, const float4* pos, const float4* v
                              float4* vel_out, int32_t* pid_out, double* pos64_out,
                              float4* force_out, RareList rare) {
     if (L.n == 0) return cudaSuccess;
-    return launch_force_pass<false>(L, L.n, pos, vel, rho, fin, pid, pos64, vstart, vcount,
+    return launch_force_pass<kBySlot>(L, L.n, pos, vel, rho, fin, pid, pos64, vstart, vcount,
                                     scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
                                     force_out, PidRange{}, rare);
 }
@@ -970,13 +1023,19 @@ cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const flo
                                    const int32_t* vcount, const int32_t* scene_step, NbrList nbr,
                                    float4* pos_out, float4* vel_out, int32_t* pid_out,
                                    double* pos64_out, PidRange range, RareList rare) {
-    const int m = range.i1 - range.i0;
+    const int m = range.slots ? range.n_slots : range.i1 - range.i0;
     if (m <= 0) return cudaSuccess;
-    if (range.i0 < 0 || range.i1 > L.n || !range.slot_of || !range.pos || !range.vel)
+    if (m > L.n ||
+        (!range.slots && (range.i0 < 0 || range.i1 > L.n || !range.slot_of || !range.pos ||
+                          !range.vel)))
         return cudaErrorInvalidValue;
-    return launch_force_pass<true>(L, m, pos, vel, rho, fin, pid, pos64, vstart, vcount,
-                                   scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
-                                   nullptr, range, rare);
+    if (range.slots)
+        return launch_force_pass<kByList>(L, m, pos, vel, rho, fin, pid, pos64, vstart, vcount,
+                                          scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
+                                          nullptr, range, rare);
+    return launch_force_pass<kByRow>(L, m, pos, vel, rho, fin, pid, pos64, vstart, vcount,
+                                     scene_step, nbr, pos_out, vel_out, pid_out, pos64_out,
+                                     nullptr, range, rare);
 }
 
 cudaError_t launch_neighbours(const Launch& L, const float4* pos, const int32_t* vstart,

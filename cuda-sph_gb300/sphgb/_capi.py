@@ -14,7 +14,7 @@ from . import _build
 MODE_BOX, MODE_PIPE = 0, 1
 WALK_CEIL, WALK_TRUNCATED = 0, 1
 DENSITY_WARP, DENSITY_THREAD = 0, 1
-HOST_ORDER_AUTO, HOST_ORDER_SLOT, HOST_ORDER_PARTICLE = 0, 1, 2
+HOST_ORDER_AUTO, HOST_ORDER_SLOT, HOST_ORDER_PARTICLE, HOST_ORDER_PIPELINED = 0, 1, 2, 3
 # checked-mode bits of the error word (sphgb_ctx_set_checks)
 CHECK_NONFINITE_INPUT, CHECK_OUT_OF_DOMAIN, CHECK_VOXEL_TABLE = 1, 2, 4
 CHECK_NEIGHBOUR_LIST, CHECK_NONFINITE_OUTPUT = 8, 16

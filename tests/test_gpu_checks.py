@@ -84,14 +84,15 @@ def test_bad_inputs_set_their_bits_and_nothing_else():
     b.close()
 
 
-@pytest.mark.parametrize("order", ["slot", "particle"])
+@pytest.mark.parametrize("order", ["slot", "particle", "pipelined"])
 def test_host_entry_runs_the_checks(order):
     torch_cuda()
     from sphgb import _capi
     from sphgb.device import SceneBatch
     spec, st, nan_ids, out_ids = _bad_state()
     b = SceneBatch([spec])
-    b.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE}[order])
+    b.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE,
+                      "pipelined": _capi.HOST_ORDER_PIPELINED}[order])
     b.set_checks(True)
     b.compute_next_state_host(st.position, st.velocity)
     bits, first, _ = b.check_word()

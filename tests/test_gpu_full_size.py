@@ -139,7 +139,7 @@ def test_full_size_fused_step_bit_identical_to_stages(fused2, stages2):
     np.testing.assert_array_equal(out.position, g["position_out"])
 
 
-@pytest.mark.parametrize("order", ["slot", "particle"])
+@pytest.mark.parametrize("order", ["slot", "particle", "pipelined"])
 def test_full_size_host_entry_bit_identical_to_device_path(config2, fused2, order):
     torch_cuda()
     from sphgb import _capi
@@ -147,7 +147,8 @@ def test_full_size_host_entry_bit_identical_to_device_path(config2, fused2, orde
     spec, st = config2
     out, _, _ = fused2
     host = SceneBatch([spec])
-    host.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE}[order])
+    host.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE,
+                         "pipelined": _capi.HOST_ORDER_PIPELINED}[order])
     pos, vel, rho = host.compute_next_state_host(st.position, st.velocity)
     host.close()
     np.testing.assert_array_equal(pos, out.position)

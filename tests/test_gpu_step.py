@@ -106,13 +106,15 @@ def test_host_entry_matches_oracle():
     assert strat.old_state is st and strat.new_state is out and strat.dt == 1 / spec.params.fps
 
 
-@pytest.mark.parametrize("order", ["slot", "particle", "auto"])
-@pytest.mark.parametrize("name", ["config0", "pipe", "sparse"])
+@pytest.mark.parametrize("order", ["slot", "particle", "pipelined", "auto"])
+@pytest.mark.parametrize("name", ["config0", "pipe", "sparse", "uncapped", "truncated"])
 def test_host_entry_bit_identical_to_device_path(name, order):
     """Calls of sphgb_compute_next_state_host in a row (uploads and downloads
-    spread over two streams; the force pass in slot order, in particle-order
-    ranges, or chosen by timing both) give the same bits as loading the state
-    and stepping it on the device."""
+    spread over streams; the force pass in slot order, in particle-order
+    ranges, in ranges pipelined behind a density pass in buckets, or chosen by
+    timing all three) give the same bits as loading the state and stepping it
+    on the device.  The uncapped and truncated scenes cannot be pipelined and
+    fall back to particle order."""
     torch_cuda()
     from sphgb import _capi
     from sphgb.device import SceneBatch
@@ -121,9 +123,10 @@ def test_host_entry_bit_identical_to_device_path(name, order):
     dev.load_states([st])
     host = SceneBatch([spec])
     host.set_host_order({"slot": _capi.HOST_ORDER_SLOT, "particle": _capi.HOST_ORDER_PARTICLE,
+                         "pipelined": _capi.HOST_ORDER_PIPELINED,
                          "auto": _capi.HOST_ORDER_AUTO}[order])
     pos, vel = st.position, st.velocity
-    for _ in range(5 if order == "auto" else 2):   # auto: warm-up, both timed orders, choice
+    for _ in range(6 if order == "auto" else 2):   # auto: warm-up, three timed orders, choice
         dev.step(1)
         want = dev.states()[0]
         pos, vel, rho = host.compute_next_state_host(pos, vel)
@@ -134,24 +137,27 @@ def test_host_entry_bit_identical_to_device_path(name, order):
     host.close()
 
 
-@pytest.mark.parametrize("shape", [(3, 7, 5), (1, 5, 1)])
+@pytest.mark.parametrize("shape", [(3, 7, 5), (1, 5, 1), (9, 11, 7)])
 def test_host_entry_particle_ranges_uneven_counts(shape):
     """Particle-order ranges when the particle count does not split evenly
     into the ranges (105 particles), or is below their number (5 particles:
-    some ranges empty): same bits as the slot-order call."""
+    some ranges empty): same bits as the slot-order call.  The pipelined
+    order runs on 693 particles (uneven ranges and buckets) and falls back to
+    particle order on the two smaller scenes."""
     torch_cuda()
     from sphgb import _capi, scenes
     from sphgb.device import SceneBatch
     nx, ny, nz = shape
     spec, st = scenes.box_dam_break(nx=nx, ny=ny, nz=nz, seed=21)
     outs = []
-    for order in (_capi.HOST_ORDER_SLOT, _capi.HOST_ORDER_PARTICLE):
+    for order in (_capi.HOST_ORDER_SLOT, _capi.HOST_ORDER_PARTICLE, _capi.HOST_ORDER_PIPELINED):
         b = SceneBatch([spec])
         b.set_host_order(order)
         outs.append(b.compute_next_state_host(st.position, st.velocity))
         b.close()
-    for a, c in zip(*outs):
-        np.testing.assert_array_equal(a, c)
+    for other in outs[1:]:
+        for a, c in zip(outs[0], other):
+            np.testing.assert_array_equal(a, c)
 
 
 def test_trajectory_config0_200_steps():
@@ -338,7 +344,7 @@ def test_host_entry_page_locked_buffers_match_pageable():
 
 
 def test_host_order_rejects_unknown_values():
-    """sphgb_ctx_set_host_order takes AUTO, SLOT or PARTICLE only; a refused
+    """sphgb_ctx_set_host_order takes AUTO, SLOT, PARTICLE or PIPELINED only; a refused
     value leaves the context usable and its results unchanged."""
     torch_cuda()
     from sphgb import _capi
