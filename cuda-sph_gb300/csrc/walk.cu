@@ -181,20 +181,19 @@ __device__ __forceinline__ unsigned reach_mask(const float4& p, int vx, int vy, 
 
 // Per warp.  An accepted entry is its slot and its squared distance (int
 // bits), the distance the candidate loop decided on, so the density term
-// needs no second gather of the neighbour's position.  Phase (a) replaces the
-// distance with the term (kSelfTerm for the particle itself).  Rows are 33
-// words apart: phase (b) reads one row per lane without bank conflicts.
+// needs no second gather of the neighbour's position; the candidate loop
+// writes both with one 8-byte store.  Phase (a) replaces the distance with
+// the term (kSelfTerm for the particle itself).
 static_assert(kTaskRun <= 16 && kTaskRun <= kSumSplit, "phase (b) gives each home two lanes");
 struct WcShared {
     float4 home[kTaskRun];
-    int32_t slot[kTaskRun][kWcList + 1];
-    int32_t dd[kTaskRun][kWcList + 1];
+    int2 e[kTaskRun][kWcList + 1];   // (slot, squared distance or term)
     int32_t off[27];    // first slot - first walk index of each non-empty walk voxel, by rank
 };
 
 // The candidate loop of k_density_wc for one task: batches of kWcBatch
 // candidates in walk order, each tested against every home particle still
-// below the cap.  Accepted entries go to S.slot[i] and S.dd[i] in walk order
+// below the cap.  Accepted entries go to S.e[i] in walk order
 // and the counts to cnt (lane i: home particle i).  Lane k < 27 holds walk voxel k's first
 // walk index Pk and member count ck.  kCull: a home particle skips the batches
 // that lie wholly in walk voxels outside its reach mask.
@@ -261,7 +260,7 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
                 band_seen |= !acc && d2 <= h2_hi;
                 const unsigned m = __ballot_sync(full, acc);
                 const int ru = r + __popc(m & lt);
-                if (acc && ru < cap) { S.slot[i][ru] = sj[u]; S.dd[i][ru] = __float_as_int(d2); }
+                if (acc && ru < cap) S.e[i][ru] = make_int2(sj[u], __float_as_int(d2));
                 r += __popc(m);
             }
             if (lane == i) cnt = r;
@@ -280,7 +279,7 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
                         acc = within_exact(ph.x, ph.y, ph.z, pj[u].x, pj[u].y, pj[u].z, h_d);
                     const unsigned m = __ballot_sync(full, acc);
                     const int ru = r + __popc(m & lt);
-                    if (acc && ru < cap) { S.slot[i][ru] = sj[u]; S.dd[i][ru] = __float_as_int(d2); }
+                    if (acc && ru < cap) S.e[i][ru] = make_int2(sj[u], __float_as_int(d2));
                     r += __popc(m);
                 }
                 if (lane == i) cnt = r;
@@ -329,9 +328,9 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home)   // S.slot[lane] serves as its row buffer
+            if (home)   // S.e[lane] serves as its row buffer
                 density_one<kLayout>(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
-                                     &S.slot[lane][0], 1);
+                                     &S.e[lane][0].x, 1);
             __syncwarp();
             continue;
         }
@@ -404,7 +403,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             for (int e = 0; e < 2; ++e) {
                 const int i = i0 + e;   // i0 even and < c_t <= kTaskRun: i < kTaskRun
                 const int na_i = i < c_t ? min(__shfl_sync(full, cnt, i), cap) : 0;
-                en[e] = lane < na_i ? make_int2(S.slot[i][lane], S.dd[i][lane]) : make_int2(-1, 0);
+                en[e] = lane < na_i ? S.e[i][lane] : make_int2(-1, 0);
             }
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
@@ -422,7 +421,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
                         if (nbr.idx)
                             nbr.idx[(size_t)si * kListCap + lane - __popc(self & lt)] = j;
                     }
-                    S.dd[i][lane] = term;
+                    S.e[i][lane].y = term;
                 }
             }
         }
@@ -439,7 +438,7 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             if (ih < c_t) {
                 const int k1 = upper ? na : min(na, kSumSplit);
                 for (int k = upper ? kSumSplit : 0; k < k1; ++k) {
-                    const int term = S.dd[ih][k];
+                    const int term = S.e[ih][k].y;
                     if (term == kSelfTerm) continue;
                     acc.add(__int_as_float(term));
                     ++others;
