@@ -1527,8 +1527,8 @@ int host_order_for_call(const SphgbCtx* c) {
 }
 }  // namespace
 
-int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
-                                  double* h_pos_out, double* h_vel_out, double* h_rho_out) {
+static int host_entry(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
+                      double* h_pos_out, double* h_vel_out, double* h_rho_out) {
     if (!ctx) return fail(SPHGB_ERR_INVALID, "ctx is null");
     if (ctx->n_scenes != 1) return fail(SPHGB_ERR_INVALID, "host entry needs a one-scene context");
     const size_t N = (size_t)ctx->n;
@@ -1700,6 +1700,19 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
     SPHGB_CUDA(cudaStreamSynchronize(st));
     record_time();
     return SPHGB_OK;
+}
+
+int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
+                                  double* h_pos_out, double* h_vel_out, double* h_rho_out) {
+    const int rc = host_entry(ctx, h_pos, h_vel, h_pos_out, h_vel_out, h_rho_out);
+    if (rc && ctx) {
+        // a failed call returns only once nothing it enqueued still runs: no
+        // copy into the caller's host buffers outlives the call
+        for (cudaStream_t s : {ctx->host_stream, ctx->host_stream2, ctx->host_stream3,
+                               ctx->host_stream4, ctx->host_stream5})
+            if (s) cudaStreamSynchronize(s);
+    }
+    return rc;
 }
 
 int sphgb_ctx_set_host_order(SphgbCtx* ctx, int order) {
