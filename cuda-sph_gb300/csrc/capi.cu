@@ -199,7 +199,7 @@ struct SphgbCtx {
     int32_t* pipe_i = nullptr;
     int32_t* h_pipe = nullptr;
     size_t cap_tasks_b = 0, cap_vbucket = 0;
-    cudaStream_t host_stream3 = nullptr, host_stream4 = nullptr, host_stream5 = nullptr;
+    cudaStream_t host_stream3 = nullptr, host_stream4 = nullptr;
     cudaEvent_t pipe_ev[3 + 2 * kPipeRanges] = {};
     std::map<int, cudaGraphExec_t> graphs;
 
@@ -253,7 +253,6 @@ void free_ctx(SphgbCtx* c) {
     if (c->host_stream2) cudaStreamDestroy(c->host_stream2);
     if (c->host_stream3) cudaStreamDestroy(c->host_stream3);
     if (c->host_stream4) cudaStreamDestroy(c->host_stream4);
-    if (c->host_stream5) cudaStreamDestroy(c->host_stream5);
     for (cudaEvent_t e : c->pipe_ev)
         if (e) cudaEventDestroy(e);
     if (c->tasks_b) cudaFree(c->tasks_b);
@@ -399,12 +398,12 @@ __global__ void k_slot_of(const int32_t* __restrict__ pbegin, int n_scenes, int 
 // state in original particle order as FP64 AoS: one thread per output row,
 // so the writes are coalesced (they may go to mapped host memory)
 __global__ void k_store_aos(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
-                            int n_scenes, int i0, int n, const float4* __restrict__ pos,
+                            int n_scenes, int n, const float4* __restrict__ pos,
                             const float4* __restrict__ vel, const float* __restrict__ rho,
                             const int32_t* __restrict__ slot_of, const double* __restrict__ pos64,
                             double* __restrict__ pos_out, double* __restrict__ vel_out,
                             double* __restrict__ rho_out) {
-    const int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int si = scene_of(i, pbegin, n_scenes);
     const int s = __ldg(slot_of + i);
@@ -1072,7 +1071,7 @@ int sphgb_ctx_store_aos_f64(SphgbCtx* ctx, double* d_pos_aos, double* d_vel_aos,
     k_slot_of<<<blocks(ctx->n), kBlock, 0, st>>>(ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                                  sep ? ctx->out_pid : ctx->pidA, ctx->slot_of);
     k_store_aos<<<blocks(ctx->n), kBlock, 0, st>>>(
-        ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n, sep ? ctx->out_pos : ctx->posA,
+        ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n, sep ? ctx->out_pos : ctx->posA,
         sep ? ctx->out_vel : ctx->velA, ctx->rho, ctx->slot_of,
         sep ? ctx->out_pos64 : ctx->pos64A, d_pos_aos, d_vel_aos, d_rho);
     SPHGB_CUDA(cudaGetLastError());
@@ -1168,6 +1167,10 @@ namespace {
 // counts, slot fill counters, slot offsets, dl.
 constexpr int kPipeK = kPipeRanges;
 constexpr int kPipeInts = 9 * kPipeK;
+// The first buckets run while the velocities are still on the host link and
+// are gathered by their own kernel; later buckets wait for the upload (done
+// by then at 4M) and gather their velocities in the density pass itself.
+constexpr int kPipeGathered = 2;
 
 __device__ __forceinline__ int range_of(int i, int n) {
     int r = 0;
@@ -1355,8 +1358,6 @@ int ensure_pipelined(SphgbCtx* c) {
     }
     if (!c->host_stream4)
         SPHGB_CUDA(cudaStreamCreateWithFlags(&c->host_stream4, cudaStreamNonBlocking));
-    if (!c->host_stream5)
-        SPHGB_CUDA(cudaStreamCreateWithFlags(&c->host_stream5, cudaStreamNonBlocking));
     for (cudaEvent_t& e : c->pipe_ev)
         if (!e) SPHGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return SPHGB_OK;
@@ -1366,15 +1367,14 @@ int ensure_pipelined(SphgbCtx* c) {
 // velocities uploaded (st2, event e_vel): the step with its force pass and
 // downloads pipelined behind the density pass (see kPipeK above).  st sorts,
 // buckets the tasks and runs the density buckets; st3, which has the
-// greatest priority, builds the slot map, gathers each bucket's velocities
-// and runs the force buckets, each after the gathers of the buckets it
+// greatest priority, builds the slot map, gathers the first buckets'
+// velocities and runs the force buckets, each after the density buckets it
 // depends on; st4 reads the counts and dependencies back and downloads each
 // range's rows.
 int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, double* sr,
                         double* h_pos_out, double* h_vel_out, double* h_rho_out) {
     const size_t N = (size_t)c->n;
-    cudaStream_t st = c->host_stream, st3 = c->host_stream3, st4 = c->host_stream4,
-                 st5 = c->host_stream5;
+    cudaStream_t st = c->host_stream, st3 = c->host_stream3, st4 = c->host_stream4;
     cudaEvent_t e_org = c->pipe_ev[0], e_bk = c->pipe_ev[1], e_dep = c->pipe_ev[2];
     cudaEvent_t* e_bucket = c->pipe_ev + 3;
     cudaEvent_t* e_range = c->pipe_ev + 3 + kPipeK;
@@ -1414,52 +1414,47 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
     SPHGB_CUDA(cudaMemcpyAsync(c->h_pipe, pi, sizeof(int32_t) * kPipeInts,
                                cudaMemcpyDeviceToHost, st4));
     SPHGB_CUDA(cudaEventRecord(e_dep, st4));
-    // the density buckets are independent of one another: they alternate
-    // between st and st5, so that one bucket's last tasks overlap the next
-    // bucket's first
-    SPHGB_CUDA(cudaStreamWaitEvent(st5, e_bk, 0));
-    const Launch L5 = c->launch(st5);
+    // The density buckets, one after another on st.  From bucket
+    // kPipeGathered on they wait for the velocity upload and gather their
+    // velocities themselves.
+    VelRows vrows;
+    vrows.vel64 = sv;
+    vrows.pid = c->pidB;
+    vrows.vel_out = c->velB;
     for (int b = 0; b < kPipeK; ++b) {
-        SPHGB_CUDA(launch_density_wc(b % 2 ? L5 : L, c->posB, nullptr, c->vstart, c->vcount,
-                                     c->rho, c->fin, c->nbr, c->tasks_b, pi + b,
-                                     pi + 2 * kPipeK + b, pi + 4 * kPipeK + b));
-        SPHGB_CUDA(cudaEventRecord(e_bucket[b], b % 2 ? st5 : st));
+        if (b == kPipeGathered) SPHGB_CUDA(cudaStreamWaitEvent(st, e_vel, 0));
+        SPHGB_CUDA(launch_density_wc(L, c->posB, nullptr, c->vstart, c->vcount, c->rho, c->fin,
+                                     c->nbr, c->tasks_b, pi + b, pi + 2 * kPipeK + b,
+                                     pi + 4 * kPipeK + b,
+                                     b >= kPipeGathered ? vrows : VelRows{}));
+        SPHGB_CUDA(cudaEventRecord(e_bucket[b], st));
     }
     c->nbr_valid = true;
-    // the slot counts and dependencies are needed on the host to launch and
-    // order the force buckets
+    // the slot counts and the dependencies are needed on the host to launch
+    // and order the force buckets
     SPHGB_CUDA(cudaEventSynchronize(e_dep));
     const int32_t* h_dep = c->h_pipe + 3 * kPipeK;
     const int32_t* h_slots = c->h_pipe + 5 * kPipeK;
     const int32_t* h_soff = c->h_pipe + 7 * kPipeK;
     const int32_t* h_dl = c->h_pipe + 8 * kPipeK;
-    int gathered = 0;   // buckets whose velocities are gathered on st3
+    int gathered = 0;   // buckets whose velocities are in slot order, as seen from st3
     auto gather_through = [&](int last) -> int {
         for (; gathered <= last; ++gathered) {
             SPHGB_CUDA(cudaStreamWaitEvent(st3, e_bucket[gathered], 0));
-            SPHGB_CUDA(launch_gather_vel_tasks(L3, c->pidB, c->tasks_b, pi + gathered,
-                                               pi + 4 * kPipeK + gathered, c->vstart, c->vcount,
-                                               sv, c->rho, c->velB, c->fin));
+            if (gathered < kPipeGathered)
+                SPHGB_CUDA(launch_gather_vel_tasks(L3, c->pidB, c->tasks_b, pi + gathered,
+                                                   pi + 4 * kPipeK + gathered, c->vstart,
+                                                   c->vcount, sv, c->rho, c->velB, c->fin));
         }
         return SPHGB_OK;
     };
-    // range r is stored in original order (FP64 rows, on st3) and downloaded
-    // once force bucket max(r, dl[r]) is done; a range's store overwrites
-    // the uploaded velocity rows of its particles, which their buckets'
-    // gathers, all at or before that force bucket, have read
-    const bool sep = c->out_pos != nullptr;
+    // range r downloads once force bucket max(r, dl[r]) is done (each force
+    // bucket writes the FP64 rows of its particles)
     int next_r = 0;
     auto download_through = [&](int b) -> int {
         for (; next_r < kPipeK && std::max(next_r, (int)h_dl[next_r]) <= b; ++next_r) {
+            SPHGB_CUDA(cudaStreamWaitEvent(st4, e_range[b], 0));
             const size_t i0 = N * next_r / kPipeK, i1 = N * (next_r + 1) / kPipeK;
-            if (i1 > i0)
-                k_store_aos<<<blocks((int)(i1 - i0)), kBlock, 0, st3>>>(
-                    c->d_scenes, c->d_pbegin, c->n_scenes, (int)i0, (int)i1,
-                    sep ? c->out_pos : c->posA, sep ? c->out_vel : c->velA, c->rho, c->slot_of,
-                    c->any_pipe ? (sep ? c->out_pos64 : c->pos64A) : nullptr, sp, sv, sr);
-            SPHGB_CUDA(cudaGetLastError());
-            SPHGB_CUDA(cudaEventRecord(e_range[next_r], st3));
-            SPHGB_CUDA(cudaStreamWaitEvent(st4, e_range[next_r], 0));
             SPHGB_CUDA(cudaMemcpyAsync(h_pos_out + 3 * i0, sp + 3 * i0,
                                        sizeof(double) * 3 * (i1 - i0), cudaMemcpyDeviceToHost,
                                        st4));
@@ -1481,8 +1476,12 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
         PidRange range;
         range.slots = c->slots_b + h_soff[b];
         range.n_slots = h_slots[b];
+        range.pos = sp;
+        range.vel = sv;
+        range.rho = sr;
         rc = enqueue_forces(c, L3, &range, b);
         if (rc) return rc;
+        SPHGB_CUDA(cudaEventRecord(e_range[b], st3));
         rc = download_through(b);
         if (rc) return rc;
     }
@@ -1498,26 +1497,30 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaStreamSynchronize(st4));
     SPHGB_CUDA(cudaStreamSynchronize(st3));
-    SPHGB_CUDA(cudaStreamSynchronize(st5));
     SPHGB_CUDA(cudaStreamSynchronize(st));
     // every slot was in exactly one bucket
     if (listed != N) return fail(SPHGB_ERR_STATE, "pipelined step: buckets missed particles");
     return SPHGB_OK;
 }
 
-// Force-pass order of the next host-entry call.  AUTO: call 1 (allocations,
-// first touches) and call 2 run in slot order, call 3 in particle order and
-// call 4 pipelined (when the context allows it); calls 2 to 4 are timed, and
-// later calls take the fastest order the context allows.
+// Force-pass order of the next host-entry call.  AUTO: calls 1 to 3 run slot
+// order, particle order and the pipelined order (when the context allows it)
+// once each, for their allocations and first kernel loads; calls 4 to 6 run
+// them again and are timed, and later calls take the fastest order the
+// context allows.
+constexpr int kAutoTimedFirst = 3;   // index of the first timed call
 int host_order_for_call(const SphgbCtx* c) {
     const bool pipe_ok = pipelined_eligible(c);
     if (c->host_order != SPHGB_HOST_ORDER_AUTO) {
         if (c->host_order == SPHGB_HOST_ORDER_PIPELINED && !pipe_ok) return SPHGB_HOST_ORDER_PARTICLE;
         return c->host_order;
     }
-    if (c->host_calls < 2) return SPHGB_HOST_ORDER_SLOT;
-    if (c->host_calls == 2) return SPHGB_HOST_ORDER_PARTICLE;
-    if (c->host_calls == 3 && pipe_ok) return SPHGB_HOST_ORDER_PIPELINED;
+    if (c->host_calls < 2 * kAutoTimedFirst) {
+        const int k = c->host_calls % kAutoTimedFirst;
+        if (k == 0) return SPHGB_HOST_ORDER_SLOT;
+        if (k == 1 || !pipe_ok) return SPHGB_HOST_ORDER_PARTICLE;
+        return SPHGB_HOST_ORDER_PIPELINED;
+    }
     int best = SPHGB_HOST_ORDER_SLOT;
     for (int o = SPHGB_HOST_ORDER_PARTICLE; o <= SPHGB_HOST_ORDER_PIPELINED; ++o)
         if (c->host_ms[o] > 0.0 && c->host_ms[o] < c->host_ms[best] &&
@@ -1625,11 +1628,11 @@ static int host_entry(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
     auto record_time = [&]() {
         const double ms = std::chrono::duration<double, std::milli>(
                               std::chrono::steady_clock::now() - t0).count();
-        if (ctx->host_calls < 1000) ++ctx->host_calls;
-        // calls 2, 3 and 4 time the three orders (call 1 warms up)
-        if (ctx->host_order == SPHGB_HOST_ORDER_AUTO && ctx->host_calls >= 2 &&
-            ctx->host_calls <= 4)
+        // calls 4 to 6 time the three orders (calls 1 to 3 warm them up)
+        if (ctx->host_order == SPHGB_HOST_ORDER_AUTO && ctx->host_calls >= kAutoTimedFirst &&
+            ctx->host_calls < 2 * kAutoTimedFirst)
             ctx->host_ms[order] = ms;
+        if (ctx->host_calls < 1000) ++ctx->host_calls;
     };
     if (order == SPHGB_HOST_ORDER_PIPELINED) {
         int rc = ensure_pipelined(ctx);
@@ -1651,7 +1654,7 @@ static int host_entry(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_slot, st2));
     SPHGB_CUDA(cudaStreamWaitEvent(st2, e_rho, 0));
-    k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0, ctx->n,
+    k_store_aos<<<nb, kBlock, 0, st2>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
                                         nullptr, nullptr, ctx->rho, ctx->slot_of, nullptr,
                                         nullptr, nullptr, sr);
     SPHGB_CUDA(cudaGetLastError());
@@ -1662,8 +1665,8 @@ static int host_entry(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
         SPHGB_CUDA(cudaEventRecord(e_done, st2));
         SPHGB_CUDA(cudaStreamWaitEvent(st, e_done, 0));
         const bool sep = ctx->out_pos != nullptr;
-        k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, 0,
-                                           ctx->n, sep ? ctx->out_pos : ctx->posA,
+        k_store_aos<<<nb, kBlock, 0, st>>>(ctx->d_scenes, ctx->d_pbegin, ctx->n_scenes, ctx->n,
+                                           sep ? ctx->out_pos : ctx->posA,
                                            sep ? ctx->out_vel : ctx->velA, nullptr, ctx->slot_of,
                                            sep ? ctx->out_pos64 : ctx->pos64A, sp, sv, nullptr);
         SPHGB_CUDA(cudaGetLastError());
@@ -1709,7 +1712,7 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
         // a failed call returns only once nothing it enqueued still runs: no
         // copy into the caller's host buffers outlives the call
         for (cudaStream_t s : {ctx->host_stream, ctx->host_stream2, ctx->host_stream3,
-                               ctx->host_stream4, ctx->host_stream5})
+                               ctx->host_stream4})
             if (s) cudaStreamSynchronize(s);
     }
     return rc;

@@ -459,15 +459,26 @@ struct NbrList {
 // particle id): particle i is at slot slot_of[i], and its next position and
 // velocity are also written as FP64 rows i of pos / vel (the host-buffer
 // entry point downloads each range while the next one is computed).
+// Velocities that the density pass gathers itself (pipelined host entry):
+// the uploaded FP64 rows in original order, converted as k_load_aos converts
+// them, into the slot-order state and the second half of the force records.
+// vel64 null: off.
+struct VelRows {
+    const double* vel64 = nullptr;   // (n, 3) FP64, scene offset + particle id
+    const int32_t* pid = nullptr;    // particle id per slot
+    float4* vel_out = nullptr;       // slot order
+};
+
 struct PidRange {
     const int32_t* slot_of = nullptr;
     int i0 = 0, i1 = 0;
     // list mode (slots set): the pass runs slots[0..n_slots) in that order
-    // instead and writes the slot-order state only (no FP64 rows)
+    // instead, each writing the rows of its particle id, density included
     const int32_t* slots = nullptr;
     int n_slots = 0;
     double* pos = nullptr;      // (n, 3) FP64
     double* vel = nullptr;      // (n, 3) FP64
+    double* rho = nullptr;      // (n,) FP64, list mode
 };
 
 // Particles a lean force pass defers to a second launch (see kForceLean in
@@ -549,7 +560,7 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
                               const int32_t* task_count, int32_t* task_next,
-                              const int32_t* task_offset = nullptr);
+                              const int32_t* task_offset = nullptr, VelRows vrows = VelRows{});
 // k_gather_vel over the slots of a bucket of density tasks
 cudaError_t launch_gather_vel_tasks(const Launch& L, const int32_t* pid, const int2* tasks,
                                     const int32_t* task_count, const int32_t* task_offset,

@@ -29,11 +29,16 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 // (vx, vy, vz, 1/rho), one 32-byte record that the force pass reads per
 // neighbour instead of three separate arrays.  With vel null only the first
 // half is written; k_gather_vel writes the second once the velocities are in.
+// first half of a force record: position and p / rho^2
+__device__ __forceinline__ float4 force_record_a(const float4& pi, const SceneDev& sc, float r) {
+    const float p = sc.k * (r - sc.rho0);
+    return make_float4(pi.x, pi.y, pi.z, p / (r * r));
+}
+
 __device__ __forceinline__ void write_force_inputs(int s, const float4& pi, const SceneDev& sc,
                                                    const float4* __restrict__ vel, float r,
                                                    float4* __restrict__ fin) {
-    const float p = sc.k * (r - sc.rho0);
-    const float4 a = make_float4(pi.x, pi.y, pi.z, p / (r * r));
+    const float4 a = force_record_a(pi, sc, r);
     if (vel) {
         const float4 v = __ldg(vel + s);
         stg256(fin + 2 * s, a, make_float4(v.x, v.y, v.z, 1.0f / r));
@@ -288,8 +293,17 @@ __device__ __forceinline__ void wc_candidates(WcShared& S, int& cnt, bool home, 
     }
 }
 
-// kLayout: 0 every scene's voxel table row-major, 1 every one tiled, 2 per scene
-template <int kLayout>
+// slot s's velocity from the FP64 rows (VelRows)
+__device__ __forceinline__ float4 vel_row(const VelRows& vr, int s,
+                                          const int32_t* __restrict__ pbegin, int n_scenes) {
+    const double* r =
+        vr.vel64 + 3 * (size_t)(__ldg(pbegin + scene_of(s, pbegin, n_scenes)) + __ldg(vr.pid + s));
+    return make_float4((float)__ldg(r), (float)__ldg(r + 1), (float)__ldg(r + 2), 0.0f);
+}
+
+// kLayout: 0 every scene's voxel table row-major, 1 every one tiled, 2 per scene.
+// kGather: the task's velocities too, from FP64 rows (vrows).
+template <int kLayout, bool kGather>
 __global__ void __launch_bounds__(kWcWarps * 32, 4)
 k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbegin,
              int n_scenes, int n, const float4* __restrict__ pos,
@@ -297,7 +311,8 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
              const int32_t* __restrict__ vcount, float* __restrict__ rho,
              float4* __restrict__ fin, NbrList nbr,
              const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
-             int32_t* __restrict__ task_next, const int32_t* __restrict__ task_offset) {
+             int32_t* __restrict__ task_next, const int32_t* __restrict__ task_offset,
+             VelRows vrows) {
     __shared__ WcShared sh[kWcWarps];
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -328,9 +343,15 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
         if (local == sc.v_count || cap > kListCap) {
             // overflow bucket (non-finite positions) or a cap beyond the shared
             // list: thread-private walk per particle
-            if (home)   // S.e[lane] serves as its row buffer
+            if (home) {   // S.e[lane] serves as its row buffer
                 density_one<kLayout>(s, pi, sc, pos, vel, vstart, vcount, n, rho, fin, nbr,
                                      &S.e[lane][0].x, 1);
+                if (kGather) {
+                    const float4 v = vel_row(vrows, s, pbegin, n_scenes);
+                    vrows.vel_out[s] = v;
+                    fin[2 * s + 1] = make_float4(v.x, v.y, v.z, 1.0f / rho[s]);
+                }
+            }
             __syncwarp();
             continue;
         }
@@ -452,7 +473,14 @@ k_density_wc(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pb
             if (home) {
                 const float r = (acc.s * sc.w_const) * sc.mass;
                 rho[s] = r;
-                if (fin) write_force_inputs(s, pi, sc, vel, r, fin);
+                if (kGather) {
+                    const float4 v = vel_row(vrows, s, pbegin, n_scenes);
+                    vrows.vel_out[s] = v;
+                    stg256(fin + 2 * s, force_record_a(pi, sc, r),
+                           make_float4(v.x, v.y, v.z, 1.0f / r));
+                } else if (fin) {
+                    write_force_inputs(s, pi, sc, vel, r, fin);
+                }
                 if (nbr.count) nbr.count[s] = others;
             }
         }
@@ -720,7 +748,8 @@ constexpr int kForceAll = 0, kForceLean = 1, kForceRare = 2;
 // Which particles a force launch runs: every slot (kBySlot); the particles of
 // rows range.i0..i1 in original order, which also write the FP64 rows of the
 // next position and velocity (kByRow); or the slots range.slots[0..n_slots)
-// (kByList), which write the slot-order state only, like kBySlot.
+// (kByList), which also write the FP64 rows of the next position, velocity
+// and density, each at its particle's id.
 constexpr int kBySlot = 0, kByRow = 1, kByList = 2;
 
 // forces + integrating_kernel (base_kernels.py:30-53) + wall response
@@ -745,8 +774,10 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
     // particle per thread (the body runs once)
     const int m_rare = kMode == kForceRare ? *rare.count : 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
-        // deferred particles are listed by row (kByRow) or by slot
+        // deferred particles are listed by row (kByRow) or by slot; rows_out:
+        // the FP64 rows are written too
         constexpr bool by_row = kIdx == kByRow;
+        constexpr bool rows_out = kIdx != kBySlot;
         int s, row = 0;
         if (kMode == kForceRare) {
             if (k >= m_rare) return;
@@ -764,6 +795,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             if (s >= n) return;
         }
         const int si = scene_of(s, pbegin, n_scenes);
+        if (kIdx == kByList) row = __ldg(pbegin + si) + __ldg(pid + s);
         const SceneDev& sc = scenes[si];
         if (kMode != kForceRare && scene_frozen(step_limit, scene_step, si)) {
             // frozen scene: the state is copied through unchanged (the sort
@@ -779,11 +811,12 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                     if (sc.mode == 1) x64[a] = pos64[3 * s + a];
                 }
             }
-            if (by_row) {
+            if (rows_out) {
                 for (int a = 0; a < 3; ++a) range.pos[3 * (size_t)row + a] = x64[a];
                 range.vel[3 * (size_t)row + 0] = v4.x;
                 range.vel[3 * (size_t)row + 1] = v4.y;
                 range.vel[3 * (size_t)row + 2] = v4.z;
+                if (kIdx == kByList) range.rho[row] = (double)__ldg(rho + s);
             }
             if (force_out) force_out[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             return;   // one particle per thread outside kForceRare
@@ -840,7 +873,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                 pos64_out[3 * s + 1] = x[1];
                 pos64_out[3 * s + 2] = x[2];
             }
-            if (by_row) {
+            if (rows_out) {
                 range.pos[3 * (size_t)row + 0] = x[0];
                 range.pos[3 * (size_t)row + 1] = x[1];
                 range.pos[3 * (size_t)row + 2] = x[2];
@@ -859,15 +892,16 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             for (int a = 0; a < 3; ++a) {
                 v[a] = (float)vd[a];
                 pos64_out[3 * s + a] = x[a];
-                if (by_row) range.pos[3 * (size_t)row + a] = x[a];
+                if (rows_out) range.pos[3 * (size_t)row + a] = x[a];
             }
             pos_out[s] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
         }
         vel_out[s] = make_float4(v[0], v[1], v[2], 0.0f);
-        if (by_row) {
+        if (rows_out) {
             range.vel[3 * (size_t)row + 0] = v[0];
             range.vel[3 * (size_t)row + 1] = v[1];
             range.vel[3 * (size_t)row + 2] = v[2];
+            if (kIdx == kByList) range.rho[row] = (double)rho_i;
         }
         pid_out[s] = p_id;
         if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
@@ -915,16 +949,23 @@ cudaError_t launch_density_wc(const Launch& L, const float4* pos, const float4* 
                               const int32_t* vstart, const int32_t* vcount, float* rho,
                               float4* fin, NbrList nbr, const int2* tasks,
                               const int32_t* task_count, int32_t* task_next,
-                              const int32_t* task_offset) {
+                              const int32_t* task_offset, VelRows vrows) {
     if (L.n == 0) return cudaSuccess;
     // persistent grid: up to 4 blocks of 8 warps per SM, warps take tasks in turn
     int blocks = (L.n + 32 * kWcWarps - 1) / (32 * kWcWarps);
     const int top = device_sm_count() * 4;
     if (blocks > top) blocks = top;
-    auto kernel = L.layout == 1 ? k_density_wc<1> : L.layout == 2 ? k_density_wc<2> : k_density_wc<0>;
+    // the velocity gather is its own instantiation: the step's kernel stays as it is
+    auto kernel = vrows.vel64
+                      ? (L.layout == 1   ? k_density_wc<1, true>
+                         : L.layout == 2 ? k_density_wc<2, true>
+                                         : k_density_wc<0, true>)
+                      : (L.layout == 1   ? k_density_wc<1, false>
+                         : L.layout == 2 ? k_density_wc<2, false>
+                                         : k_density_wc<0, false>);
     kernel<<<blocks, kWcWarps * 32, 0, L.stream>>>(L.scenes, L.pbegin, L.n_scenes, L.n, pos, vel,
                                                    vstart, vcount, rho, fin, nbr, tasks, task_count,
-                                                   task_next, task_offset);
+                                                   task_next, task_offset, vrows);
     return cudaGetLastError();
 }
 
@@ -1024,9 +1065,8 @@ cudaError_t launch_integrate_range(const Launch& L, const float4* pos, const flo
                                    double* pos64_out, PidRange range, RareList rare) {
     const int m = range.slots ? range.n_slots : range.i1 - range.i0;
     if (m <= 0) return cudaSuccess;
-    if (m > L.n ||
-        (!range.slots && (range.i0 < 0 || range.i1 > L.n || !range.slot_of || !range.pos ||
-                          !range.vel)))
+    if (m > L.n || !range.pos || !range.vel ||
+        (range.slots ? !range.rho : (range.i0 < 0 || range.i1 > L.n || !range.slot_of)))
         return cudaErrorInvalidValue;
     if (range.slots)
         return launch_force_pass<kByList>(L, m, pos, vel, rho, fin, pid, pos64, vstart, vcount,

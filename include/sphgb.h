@@ -190,15 +190,17 @@ int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const doub
  * state is downloaded whole.  SPHGB_HOST_ORDER_PARTICLE: original particle
  * order in ranges, each range's rows downloaded while the next range is
  * computed; faster when nearby particle ids are nearby in space, slower when
- * they are scattered.  SPHGB_HOST_ORDER_PIPELINED: the same ranges, with the
- * density pass run in buckets of the ranges' particles; a range's forces and
- * downloads start once every bucket its particles' neighbours fall in is
- * done, while later buckets are still running (when ids follow space, most
- * of the download overlaps the density pass).  It needs a scene with a
- * neighbour cap of at most 32, the reference's walk dims set to
- * SPHGB_WALK_CEIL, the warp density kernel and at least 512 particles, and
- * is particle order otherwise.  SPHGB_HOST_ORDER_AUTO (default): call 1 warms
- * up, calls 2 to 4 time the three orders and later calls take the fastest.
+ * they are scattered.  SPHGB_HOST_ORDER_PIPELINED: the density pass in 16
+ * buckets of tasks by the particle-id range of their first particle, the
+ * force pass over each bucket's slots once every bucket its particles'
+ * neighbours fall in is done, and each range's rows downloaded as soon as
+ * the buckets holding its particles are, while later buckets are still
+ * running (when ids follow space, most of the download overlaps the density
+ * pass).  It needs one scene with a neighbour cap of at most 32, the
+ * reference's walk dims set to SPHGB_WALK_CEIL, the warp density kernel, at
+ * least 512 particles and no step limits, and is particle order otherwise.
+ * SPHGB_HOST_ORDER_AUTO (default): calls 1 to 3 run the three orders once,
+ * calls 4 to 6 time them and later calls take the fastest.
  * No counterpart in the reference (its step is synchronous,
  * abstract_sph_strategy.py:31-46). */
 enum { SPHGB_HOST_ORDER_AUTO = 0, SPHGB_HOST_ORDER_SLOT = 1, SPHGB_HOST_ORDER_PARTICLE = 2,

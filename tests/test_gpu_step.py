@@ -126,7 +126,7 @@ def test_host_entry_bit_identical_to_device_path(name, order):
                          "pipelined": _capi.HOST_ORDER_PIPELINED,
                          "auto": _capi.HOST_ORDER_AUTO}[order])
     pos, vel = st.position, st.velocity
-    for _ in range(6 if order == "auto" else 2):   # auto: warm-up, three timed orders, choice
+    for _ in range(8 if order == "auto" else 2):   # auto: three orders run, timed, then chosen
         dev.step(1)
         want = dev.states()[0]
         pos, vel, rho = host.compute_next_state_host(pos, vel)
