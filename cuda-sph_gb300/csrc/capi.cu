@@ -1172,9 +1172,30 @@ constexpr int kPipeInts = 9 * kPipeK;
 // by then at 4M) and gather their velocities in the density pass itself.
 constexpr int kPipeGathered = 2;
 
-__device__ __forceinline__ int range_of(int i, int n) {
+// Range r of the original indices is [b[r], b[r + 1]).  The last ranges are
+// smaller: the force buckets and downloads that must wait for the end of the
+// density pass are short.  Relative sizes of the ranges:
+constexpr int kPipeWeight[kPipeK] = {4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 4, 2, 1, 1};
+struct PipeBounds {
+    int32_t b[kPipeK + 1];
+};
+
+PipeBounds pipe_bounds(int n) {
+    int64_t total = 0;
+    for (int w : kPipeWeight) total += w;
+    PipeBounds pb;
+    int64_t acc = 0;
+    pb.b[0] = 0;
+    for (int r = 0; r < kPipeK; ++r) {
+        acc += kPipeWeight[r];
+        pb.b[r + 1] = (int32_t)((int64_t)n * acc / total);
+    }
+    return pb;
+}
+
+__device__ __forceinline__ int range_of(int i, const PipeBounds& pb) {
     int r = 0;
-    while (r + 1 < kPipeK && i >= (int)(((int64_t)n * (r + 1)) / kPipeK)) ++r;
+    while (r + 1 < kPipeK && i >= pb.b[r + 1]) ++r;
     return r;
 }
 
@@ -1188,7 +1209,7 @@ __device__ __forceinline__ int task_size(int2 t, const int32_t* __restrict__ vst
 // per bucket and block, not one per task on kPipeK shared addresses.
 __global__ void k_bucket_count(const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
                                const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
-                               const int32_t* __restrict__ vcount, int n,
+                               const int32_t* __restrict__ vcount, PipeBounds pb,
                                int32_t* __restrict__ pi) {
     __shared__ int h[kPipeK], hs[kPipeK];
     if (threadIdx.x < kPipeK) h[threadIdx.x] = hs[threadIdx.x] = 0;
@@ -1196,7 +1217,7 @@ __global__ void k_bucket_count(const int2* __restrict__ tasks, const int32_t* __
     const int m = *task_count;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
         const int2 t = tasks[k];
-        const int b = range_of(pid[t.y], n);
+        const int b = range_of(pid[t.y], pb);
         atomicAdd(h + b, 1);
         atomicAdd(hs + b, task_size(t, vstart, vcount));
     }
@@ -1211,7 +1232,8 @@ __global__ void k_bucket_count(const int2* __restrict__ tasks, const int32_t* __
 // the tasks' voxel order up to the order in which blocks take their places.
 __global__ void k_bucket_scatter(const int2* __restrict__ tasks, const int32_t* __restrict__ task_count,
                                  const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
-                                 const int32_t* __restrict__ vcount, int n, int32_t* __restrict__ pi,
+                                 const int32_t* __restrict__ vcount, PipeBounds pb,
+                                 int32_t* __restrict__ pi,
                                  int2* __restrict__ tasks_b, int32_t* __restrict__ slots_b,
                                  int32_t* __restrict__ vbucket) {
     __shared__ int cnt[kPipeK], scnt[kPipeK], base[kPipeK], sbase[kPipeK];
@@ -1236,7 +1258,7 @@ __global__ void k_bucket_scatter(const int2* __restrict__ tasks, const int32_t* 
         int b = -1, local = 0, slocal = 0, sz = 0;
         if (k < m) {
             t = tasks[k];
-            b = range_of(pid[t.y], n);
+            b = range_of(pid[t.y], pb);
             sz = task_size(t, vstart, vcount);
             local = atomicAdd(cnt + b, 1);
             slocal = atomicAdd(scnt + b, sz);
@@ -1264,7 +1286,7 @@ __global__ void k_bucket_deps(const SceneDev* __restrict__ scenes, const int2* _
                               const int32_t* __restrict__ task_count,
                               const int32_t* __restrict__ pid, const int32_t* __restrict__ vstart,
                               const int32_t* __restrict__ vcount,
-                              const int32_t* __restrict__ vbucket, int n,
+                              const int32_t* __restrict__ vbucket, PipeBounds pb,
                               int32_t* __restrict__ pi) {
     __shared__ int dep[kPipeK], dl[kPipeK];
     if (threadIdx.x < kPipeK) dep[threadIdx.x] = dl[threadIdx.x] = -1;
@@ -1274,12 +1296,12 @@ __global__ void k_bucket_deps(const SceneDev* __restrict__ scenes, const int2* _
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
         const int2 t = tasks[k];
         const int vid = t.x;
-        const int b = range_of(pid[t.y], n);
+        const int b = range_of(pid[t.y], pb);
         int need = vbucket[vid];
         const int local = vid - sc.v_begin;
         if (local == sc.v_count) {      // the overflow entry: no neighbours, ids unordered
             const int end = t.y + task_size(t, vstart, vcount);
-            for (int d = t.y; d < end; ++d) atomicMax(dl + range_of(pid[d], n), b);
+            for (int d = t.y; d < end; ++d) atomicMax(dl + range_of(pid[d], pb), b);
         } else {
             const Udiv q0{sc.div_m[0], sc.div_s[0]}, q1{sc.div_m[1], sc.div_s[1]};
             int vx, vy, vz;
@@ -1402,12 +1424,13 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
     const int grid = device_sm_count() * 4;
     SPHGB_CUDA(cudaMemsetAsync(pi, 0, sizeof(int32_t) * kPipeInts, st));
     SPHGB_CUDA(cudaMemsetAsync(c->vbucket, 0xff, sizeof(int32_t) * c->v_total, st));
-    k_bucket_count<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount,
-                                            c->n, pi);
+    const PipeBounds pb = pipe_bounds(c->n);
+    k_bucket_count<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount, pb,
+                                            pi);
     k_bucket_scatter<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount,
-                                              c->n, pi, c->tasks_b, c->slots_b, c->vbucket);
+                                              pb, pi, c->tasks_b, c->slots_b, c->vbucket);
     k_bucket_deps<<<grid, kBlock, 0, st>>>(c->d_scenes, c->tasks_b, n_tasks, c->pidB, c->vstart,
-                                           c->vcount, c->vbucket, c->n, pi);
+                                           c->vcount, c->vbucket, pb, pi);
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_bk, st));
     SPHGB_CUDA(cudaStreamWaitEvent(st4, e_bk, 0));
@@ -1454,7 +1477,7 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
     auto download_through = [&](int b) -> int {
         for (; next_r < kPipeK && std::max(next_r, (int)h_dl[next_r]) <= b; ++next_r) {
             SPHGB_CUDA(cudaStreamWaitEvent(st4, e_range[b], 0));
-            const size_t i0 = N * next_r / kPipeK, i1 = N * (next_r + 1) / kPipeK;
+            const size_t i0 = (size_t)pb.b[next_r], i1 = (size_t)pb.b[next_r + 1];
             SPHGB_CUDA(cudaMemcpyAsync(h_pos_out + 3 * i0, sp + 3 * i0,
                                        sizeof(double) * 3 * (i1 - i0), cudaMemcpyDeviceToHost,
                                        st4));
