@@ -1404,19 +1404,18 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
     const Launch L3 = c->launch(st3);
     double* p64A = c->any_pipe ? c->pos64A : nullptr;
     double* p64B = c->any_pipe ? c->pos64B : nullptr;
-    // sort (the velocities follow after the density pass, per bucket)
+    // sort (the velocities follow bucket by bucket: gathered into slot order
+    // by the density buckets themselves, or for the first buckets by a kernel
+    // of their own on st3)
     int rc = enqueue_organize(c, L, c->posA, nullptr, c->pidA, p64A, c->posB, c->velB, c->pidB,
                               p64B, c->vstart, c->vcount, nullptr, true, true);
     if (rc) return rc;
     SPHGB_CUDA(cudaEventRecord(e_org, st));
-    // st3: original index -> slot (the deferred particles of the force pass
-    // are listed by row), then the velocity upload; the gathers read its FP64
-    // rows, and a force bucket overwrites only the rows of its own
-    // particles, which its gathers have read
+    // st3 after the sort and the velocity upload: the gathers and the
+    // density buckets read the upload's FP64 rows, and a force bucket
+    // overwrites only the rows of its own particles, whose velocities its
+    // density bucket (or gather) has already read
     SPHGB_CUDA(cudaStreamWaitEvent(st3, e_org, 0));
-    k_slot_of<<<blocks(c->n), kBlock, 0, st3>>>(c->d_pbegin, c->n_scenes, c->n, c->pidB,
-                                                 c->slot_of);
-    SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaStreamWaitEvent(st3, e_vel, 0));
     // buckets and dependencies
     int32_t* pi = c->pipe_i;
