@@ -181,8 +181,10 @@ int sphgb_ctx_step_profiled(SphgbCtx* ctx, int n_steps, void* stream, float* h_s
  * AoS state out, synchronous (AbstractSPHStrategy.compute_next_state,
  * abstract_sph_strategy.py:31-46, including its host<->device copies at
  * :65-74 and :77-84).  Context must hold exactly one scene.  Host buffers may
- * be pageable or page-locked (page-locked copies faster); they are copied
- * through device staging buffers. */
+ * be pageable or page-locked (page-locked copies faster, and only they let
+ * the copies overlap the step); they are copied through device staging
+ * buffers.  A call that fails returns only after every copy it started has
+ * finished. */
 int sphgb_compute_next_state_host(SphgbCtx* ctx, const double* h_pos, const double* h_vel,
                                   double* h_pos_out, double* h_vel_out, double* h_rho_out);
 /* Order in which sphgb_compute_next_state_host runs its force pass (results
