@@ -1428,11 +1428,15 @@ int host_step_pipelined(SphgbCtx* c, cudaEvent_t e_vel, double* sp, double* sv, 
                                             pi);
     k_bucket_scatter<<<grid, kBlock, 0, st>>>(c->tasks, n_tasks, c->pidB, c->vstart, c->vcount,
                                               pb, pi, c->tasks_b, c->slots_b, c->vbucket);
-    k_bucket_deps<<<grid, kBlock, 0, st>>>(c->d_scenes, c->tasks_b, n_tasks, c->pidB, c->vstart,
-                                           c->vcount, c->vbucket, pb, pi);
     SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaEventRecord(e_bk, st));
+    // st4: the dependencies, which only the host's ordering of the force
+    // buckets needs, while st goes on with the density buckets; then the
+    // counts, offsets and dependencies to the host
     SPHGB_CUDA(cudaStreamWaitEvent(st4, e_bk, 0));
+    k_bucket_deps<<<grid, kBlock, 0, st4>>>(c->d_scenes, c->tasks_b, n_tasks, c->pidB, c->vstart,
+                                            c->vcount, c->vbucket, pb, pi);
+    SPHGB_CUDA(cudaGetLastError());
     SPHGB_CUDA(cudaMemcpyAsync(c->h_pipe, pi, sizeof(int32_t) * kPipeInts,
                                cudaMemcpyDeviceToHost, st4));
     SPHGB_CUDA(cudaEventRecord(e_dep, st4));

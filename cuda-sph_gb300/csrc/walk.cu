@@ -770,8 +770,8 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             int32_t* __restrict__ pid_out, double* __restrict__ pos64_out,
             float4* __restrict__ force_out, PidRange range, RareList rare,
             const int32_t* __restrict__ step_limit) {
-    // kForceRare: a grid-stride loop over the deferred particles; otherwise one
-    // particle per thread (the body runs once)
+    // kForceRare and kByList: a grid-stride loop over the deferred particles
+    // or the listed slots; otherwise one particle per thread (the body runs once)
     const int m_rare = kMode == kForceRare ? *rare.count : 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x;; k += gridDim.x * blockDim.x) {
         // deferred particles are listed by row (kByRow) or by slot; rows_out:
@@ -819,7 +819,8 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
                 if (kIdx == kByList) range.rho[row] = (double)__ldg(rho + s);
             }
             if (force_out) force_out[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            return;   // one particle per thread outside kForceRare
+            if (kMode == kForceRare || kIdx == kByList) continue;
+            return;   // one particle per thread outside kForceRare and kByList
         }
         // the particle's own force record holds its position and velocity too
         // (written from this state by the density pass, k_gather_vel or
@@ -842,6 +843,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
             }
             if (!ok) {
                 rare.idx[rare.base + atomicAdd(rare.count, 1)] = by_row ? row : s;
+                if (kIdx == kByList) continue;
                 return;
             }
             f = Forces{{fs.pxy.s.x, fs.pxy.s.y, fs.pz.s}, {fs.vxy.s.x, fs.vxy.s.y, fs.vz.s}, fs.terms};
@@ -905,7 +907,7 @@ k_integrate(const SceneDev* __restrict__ scenes, const int32_t* __restrict__ pbe
         }
         pid_out[s] = p_id;
         if (force_out) force_out[s] = make_float4(F[0], F[1], F[2], 0.0f);
-        if (kMode != kForceRare) return;
+        if (kMode != kForceRare && kIdx != kByList) return;
     }
 }
 
@@ -1019,13 +1021,18 @@ cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const f
                               const int32_t* scene_step, NbrList nbr, float4* pos_out,
                               float4* vel_out, int32_t* pid_out, double* pos64_out,
                               float4* force_out, PidRange range, RareList rare) {
+    // a slot list runs on a grid of at most 4 blocks per SM, each thread
+    // taking list entries in turn: a bucket's list is a few waves long, and
+    // no partial last wave is left
+    const int grid = kIdx == kByList ? std::min(blocks_for(m), device_sm_count() * 4)
+                                     : blocks_for(m);
     if (L.pipe_scenes) {
-        k_integrate<true, kIdx, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<true, kIdx, kForceAll><<<grid, kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
             RareList{}, L.step_limit);
     } else if (nbr.count && rare.count) {
-        k_integrate<false, kIdx, kForceLean><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<false, kIdx, kForceLean><<<grid, kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
             L.step_limit);
@@ -1036,7 +1043,7 @@ cudaError_t launch_force_pass(const Launch& L, int m, const float4* pos, const f
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range, rare,
             L.step_limit);
     } else {
-        k_integrate<false, kIdx, kForceAll><<<blocks_for(m), kBlock, 0, L.stream>>>(
+        k_integrate<false, kIdx, kForceAll><<<grid, kBlock, 0, L.stream>>>(
             L.scenes, L.pbegin, L.n_scenes, L.n, L.pipe, pos, vel, rho, fin, pid, pos64, vstart,
             vcount, scene_step, nbr, pos_out, vel_out, pid_out, pos64_out, force_out, range,
             RareList{}, L.step_limit);
